@@ -1,0 +1,375 @@
+"""Benchmark of the neural-LoD hot path on GB300 (one JSON line on stdout, rank 0).
+
+Headline workload: the throughput query forward at batch 2^21 (16-level hash grid with 2^19
+entries/level + two degree-4 SH encodings + LoD one-hot -> 80-wide input -> 4 x 64 ReLU -> 3
+exp outputs), FP16 tcgen05 form, inputs resident in HBM.  A "step" is one fused query launch
+over the whole batch.  Also reported: the same workload in the plain FP32 form, the end-to-end
+call from pinned host buffers, the visibility query (batch 65,536) and the visibility training
+step (batch 2^18, fwd + BCE + bwd + Adam) in both forms, the FP64-oracle error and a scalar FP32
+CPU baseline of the same encoding + MLP.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica of the workload on its own GPU
+(the path has no data exchange); value = total queries of all ranks / max-over-ranks time.
+Between timed steps the L2 cache is flushed by writing a 256 MiB buffer (outside the events).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "queries/s fwd & samples/s train, FP16-TC vs plain FP32, 1 GB300, err≤1e-3 vs FP64"
+UNIT = "queries/s"
+FLOP_PER_QUERY = 34176          # 2 * (72*64 + 3*64*64 + 64*3), real (unpadded) layers
+BYTES_PER_QUERY = 52            # 40 B input + 12 B output
+TRAIN_FLOP_PER_SAMPLE = 43392   # visibility_train fwd 14,464 + bwd 28,928
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while the timed region runs."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device_index: int):
+        self.proc = None
+        self.dev = device_index
+        self.out_path = Path(os.environ.get("TMPDIR", "/tmp")) / f"nlod_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.out_path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.dev)], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.out_path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out_path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        try:
+            self.out_path.unlink()
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def time_steps(fn, steps, warmup, flush=None, stream=None):
+    """Per-step CUDA-event durations (ms) of fn() on the current stream, L2 flushed in between."""
+    import torch
+
+    for _ in range(warmup):
+        if flush is not None:
+            flush()
+        fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        if flush is not None:
+            flush()
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        fn()
+        e.record()
+        times.append((s, e))
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in times]
+
+
+def traffic_from_profile():
+    """DRAM bytes per launch of the fused query kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "forward_tc_throughput_query.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(enc, net, n_in, n_out, params, x_all, target_cpu_seconds=12.0):
+    """Scalar FP32 host evaluation of the same encoding + MLP over all host threads, on a bounded
+    sample of the workload's inputs sized to ~target_cpu_seconds of CPU work."""
+    import numpy as np
+
+    import oracle
+
+    orc = oracle.Oracle(enc, net, n_in, n_out)
+    probe = x_all[:4096]
+    t0 = time.perf_counter()
+    _, threads = orc.forward_f32(probe, params)
+    dt = time.perf_counter() - t0
+    per_query_cpu = dt * threads / probe.shape[0]
+    n = int(min(x_all.shape[0], max(4096, target_cpu_seconds / max(per_query_cpu, 1e-9))))
+    n = n // 128 * 128
+    sample = np.ascontiguousarray(x_all[:n])
+    t0 = time.perf_counter()
+    _, threads = orc.forward_f32(sample, params)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {n} queries of the throughput_query batch (same inputs and weights), FP32 scalar, {threads} threads"}
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the reference's CPU implementation of the path.  tiny-cuda-nn has no CPU
+    path, so this times the FP32 restatement of its encoding + MLP (oracle port) on the host
+    cores, each step a bounded sample of the throughput_query workload."""
+    if rank != 0:
+        return
+    import numpy as np
+
+    import oracle
+    from neural_lod_gb300 import workloads as W
+
+    enc, net = W.throughput_configs()
+    orc = oracle.Oracle(enc, net, 10, 3)
+    params = W.xavier_params(orc.spec, seed=7)
+    n = 1 << 15
+    x = W.throughput_inputs(n, seed=1)
+    for _ in range(max(args.warmup, 0)):
+        orc.forward_f32(x[:4096], params)
+    times = []
+    threads = 1
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, threads = orc.forward_f32(x, params)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = n * args.steps / total
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": "throughput_query (bounded sample)", "global_batch": n, "precision": "fp32-cpu",
+                       "l2": "n/a (host)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{n} queries of the throughput_query workload per step, FP32 scalar restatement"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_env()
+
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import numpy as np
+    import torch
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import oracle
+    from neural_lod_gb300 import NetworkWithInputEncoding, workloads as W
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+
+    # ---- headline: throughput query forward, batch 2^21 ----
+    n = W.WORKLOADS["throughput_query"]["batch"]
+    enc, net = W.throughput_configs()
+    spec = oracle.model_spec(enc, net, 10, 3)
+    params = W.xavier_params(spec, seed=7 + rank)
+    x_host = W.throughput_inputs(n, seed=1 + rank)
+    x = torch.from_numpy(x_host).to(dev)
+    out = torch.empty((n, 3), device=dev)
+    m16 = NetworkWithInputEncoding(10, 3, enc, net, precision="fp16")
+    m16.set_params(params)
+    m32 = NetworkWithInputEncoding(10, 3, enc, net, precision="fp32")
+    m32.set_params(params)
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def flush():
+        flush_buf.fill_(1)
+
+    # accuracy vs the FP64 oracle on a sample of the same batch
+    ns = 4096
+    ref = oracle.Oracle(enc, net, 10, 3).forward(x_host[:ns], params)
+    m16.inference(x[:ns], out[:ns])
+    err16 = float(np.abs(out[:ns].cpu().numpy() - ref).mean())
+    m32.inference(x[:ns], out[:ns])
+    err32 = float(np.abs(out[:ns].cpu().numpy() - ref).mean())
+
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_wall0 = time.perf_counter()
+        times16 = time_steps(lambda: m16.inference(x, out), args.steps, args.warmup, flush)
+        t_wall = time.perf_counter() - t_wall0
+    clocks = clk.summary()
+    torch.cuda.synchronize()
+    m16.sync_status()
+    ms16 = statistics.mean(times16)
+    times32 = time_steps(lambda: m32.inference(x, out), max(3, args.steps // 4), 3, flush)
+    ms32 = statistics.mean(times32)
+
+    # ---- end to end through the public API from pinned host buffers ----
+    x_pin = torch.from_numpy(x_host).pin_memory()
+    out_pin = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+    x_dev2 = torch.empty_like(x)
+
+    def e2e_step():
+        x_dev2.copy_(x_pin, non_blocking=True)
+        m16.inference(x_dev2, out)
+        out_pin.copy_(out, non_blocking=True)
+
+    times_e2e = time_steps(e2e_step, max(3, args.steps // 2), 3, flush)
+    ms_e2e = statistics.mean(times_e2e)
+
+    # ---- visibility query, batch 65,536 ----
+    nv = W.WORKLOADS["visibility_query"]["batch"]
+    venc, vnet = W.visibility_configs()
+    vspec = oracle.model_spec(venc, vnet, 6, 1)
+    vparams = W.xavier_params(vspec, seed=8)
+    xv, _, frac = W.visibility_inputs(nv, seed=2)
+    xvd, fracd = torch.from_numpy(xv).to(dev), torch.from_numpy(frac).to(dev)
+    vis = {}
+    for prec in ("fp16", "fp32"):
+        mv = NetworkWithInputEncoding(6, 1, venc, vnet, precision=prec)
+        mv.set_params(vparams)
+        mv.set_max_level_gpu(fracd)
+        ov = torch.empty((nv, 1), device=dev)
+        tv = time_steps(lambda: mv.inference(xvd, ov), args.steps, 3, flush)
+        vis[prec] = nv / (statistics.mean(tv) * 1e-3)
+        del mv
+
+    # ---- visibility training step, batch 2^18 ----
+    nt = W.WORKLOADS["visibility_train"]["batch"]
+    tenc, tnet = W.visibility_configs(16)
+    tspec = oracle.model_spec(tenc, tnet, 6, 1)
+    tparams = W.xavier_params(tspec, seed=9)
+    xt, _, _ = W.visibility_inputs(nt, seed=3)
+    tt = (np.random.default_rng(3).random((nt, 1)) < 0.3).astype(np.float32)
+    xtd, ttd = torch.from_numpy(xt).to(dev), torch.from_numpy(tt).to(dev)
+    train = {}
+    for prec in ("fp16", "fp32"):
+        mt = NetworkWithInputEncoding(6, 1, tenc, tnet, loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER,
+                                      precision=prec)
+        mt.set_params(tparams)
+        lo = torch.empty(1, device=dev)
+        tr = time_steps(lambda: mt.training_step(xtd, ttd, lo), max(3, args.steps // 2), 3, flush)
+        train[prec] = nt / (statistics.mean(tr) * 1e-3)
+        del mt
+
+    # ---- aggregate over ranks ----
+    total_queries = n * world
+    t_step = ms16
+    if pg:
+        tt_ = torch.tensor([ms16, ms_e2e], device=dev)
+        pg.all_reduce(tt_, op=pg.ReduceOp.MAX)
+        t_step, ms_e2e = float(tt_[0]), float(tt_[1])
+    value = total_queries / (t_step * 1e-3)
+    e2e_value = total_queries / (ms_e2e * 1e-3)
+
+    if rank != 0:
+        if pg:
+            pg.barrier()
+        return
+
+    pk = peaks()
+    achieved_tflops = FLOP_PER_QUERY * n / (ms16 * 1e-3) / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp16", "data": "synthetic (seeded PCG64 inputs, Xavier/U[-1e-4,1e-4] weights)",
+        "config": {"workload": "throughput_query", "global_batch": n * world, "per_gpu_batch": n,
+                   "encoding": "hashgrid L16 F2 T2^19 base16 s1.5 + SH4 x2 + onehot8 (80 wide)",
+                   "mlp": "80-64-64-64-64-3 ReLU/exp", "precision": "fp16 tcgen05, fp32 accumulate",
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(x_host.nbytes),
+                "d2h_bytes_per_step": int(n * 3 * 4)},
+        "roofline": {"bound": "tensor", "achieved": achieved_tflops, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                     "frac": achieved_tflops / pk["bf16_tflops"], "traffic": traffic_from_profile(),
+                     "peak_source": pk["source"], "flop_per_query": FLOP_PER_QUERY,
+                     "hbm_frac": BYTES_PER_QUERY * n / (ms16 * 1e-3) / 1e9 / pk["hbm_gbs"]},
+        "fp32_form": {"value": n / (ms32 * 1e-3), "unit": UNIT, "ms_per_step": ms32},
+        "speedup_fp16_vs_fp32": ms32 / ms16,
+        "err_vs_fp64": {"fp16_mean_abs": err16, "fp32_mean_abs": err32, "sample": ns},
+        "visibility_query": {"batch": nv, "fp16_queries_per_s": vis["fp16"], "fp32_queries_per_s": vis["fp32"]},
+        "visibility_train": {"batch": nt, "fp16_samples_per_s": train["fp16"], "fp32_samples_per_s": train["fp32"],
+                             "flop_per_sample": TRAIN_FLOP_PER_SAMPLE},
+        "clocks": clocks,
+        "gpu_launches": len(times16),
+        "wall_s_timed_region": t_wall,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(enc, net, 10, 3, params, x_host)
+    print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,194 @@
+/*
+ * nlod.h -- C ABI of the GB300-native neural level-of-detail library (libnlod.so).
+ *
+ * The library implements the neural-LoD query and its training: a composite input
+ * encoding (multiresolution hash grid, spherical harmonics, identity, one-hot) feeding a
+ * small fully fused MLP, trained with a fused forward+loss+backward and Adam
+ * (+ ExponentialDecay / EMA wrappers).  The call shape mirrors tiny-cuda-nn's
+ * NetworkWithInputEncoding + Trainer, the API the neural_lod learner and renderers call:
+ *
+ *   tcnn::NetworkWithInputEncoding<__half>
+ *        rptr/ext/tiny-cuda-nn/include/tiny-cuda-nn/network_with_input_encoding.h:41-188
+ *   tcnn::Trainer<float, __half, __half>
+ *        rptr/ext/tiny-cuda-nn/include/tiny-cuda-nn/trainer.h:51-355
+ *   tcnn::cpp::Module (type-erased form)
+ *        rptr/ext/tiny-cuda-nn/include/tiny-cuda-nn/cpp_api.h:74-110
+ *
+ * Conventions
+ *  - Every entry point that can fail returns an int status (NLOD_OK == 0) and never
+ *    throws across the boundary; the message of the last failure on the calling thread
+ *    is returned by nlod_last_error().
+ *  - Streams are passed as void* (a cudaStream_t; NULL = legacy default stream).
+ *  - Matrices are row-per-element FP32: input [n][n_input_dims], output
+ *    [n][n_output_dims], target [n][n_output_dims].  This is tiny-cuda-nn's
+ *    column-major GPUMatrix<float> as the neural_lod callers build it
+ *    (rptr/cuda/neural-lod/neural_lod_learning_kernels.cuh:123, input_idx = i * n_in).
+ *  - Unless stated otherwise every pointer argument is a device pointer and every
+ *    call is asynchronous on the given stream.
+ *  - The batch size n must be a multiple of NLOD_BATCH_GRANULARITY (128), as in
+ *    tiny-cuda-nn (rptr/ext/tiny-cuda-nn/src/fully_fused_mlp.cu:598-602,
+ *    rptr/ext/tiny-cuda-nn/include/tiny-cuda-nn/common.h:287).
+ *  - Parameters are laid out network first, then encoding
+ *    (network_with_input_encoding.h:113-120); the MLP's matrices are row-major
+ *    [out][in], the output layer padded to 16 rows (fully_fused_mlp.cu:646-677).
+ */
+#ifndef NLOD_H
+#define NLOD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define NLOD_API __attribute__((visibility("default")))
+#else
+#define NLOD_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define NLOD_OK              0
+#define NLOD_ERR_INVALID     1  /* bad argument, size or configuration (rejected before launch) */
+#define NLOD_ERR_CUDA        2  /* a CUDA runtime call failed */
+#define NLOD_ERR_ALLOC       3  /* device or host allocation failed */
+#define NLOD_ERR_UNSUPPORTED 4  /* configuration valid for tiny-cuda-nn but not implemented here */
+#define NLOD_ERR_TIMEOUT     5  /* a bounded device-side wait gave up (error flag set by a kernel) */
+#define NLOD_ERR_STATE       6  /* call made in the wrong state (e.g. backward without forward) */
+
+/* Arithmetic form of the network. */
+#define NLOD_PRECISION_FP32  0  /* plain FP32 form: CUDA-core encoding + MLP, FP32 everything */
+#define NLOD_PRECISION_FP16  1  /* tcgen05 tensor-core MLP, FP16 operands, FP32 accumulate   */
+#define NLOD_PRECISION_BF16  2  /* tcgen05 tensor-core MLP, BF16 operands, FP32 accumulate   */
+
+#define NLOD_BATCH_GRANULARITY 128
+
+typedef struct nlod_module nlod_module;
+typedef struct nlod_ctx nlod_ctx;
+
+/* Thread-local message describing the last failure ("" if none). */
+NLOD_API const char* nlod_last_error(void);
+
+/* Library version string. */
+NLOD_API const char* nlod_version(void);
+
+/*
+ * Build a network-with-input-encoding and its trainer from tiny-cuda-nn JSON configs.
+ * Replaces `new NetworkWithInputEncoding(n_input_dims, n_output_dims, encoding, network)`
+ * + create_loss + create_optimizer + `new Trainer(network, optimizer, loss, seed)`
+ * (rptr/cuda/neural-lod/neural_lod_learning_init.cu:654-668, 889-903).
+ * loss_json / optimizer_json may be NULL (inference-only module).  Parameters are
+ * initialised from `seed` (Xavier-uniform MLP, U[-1e-4, 1e-4] grid entries).
+ * Synchronous.  Allocates all device state on the current device.
+ */
+NLOD_API int nlod_module_create(const char* encoding_json, const char* network_json,
+                       const char* loss_json, const char* optimizer_json,
+                       uint32_t n_input_dims, uint32_t n_output_dims,
+                       int precision, uint64_t seed, nlod_module** out);
+
+/*
+ * Host-only: the flattened layout the configs produce (encoded width, per nested encoding
+ * input/output columns and padding, grid offset tables, matrix shapes, parameter counts) as a
+ * malloc'ed JSON string (free with nlod_free_string).  Touches no GPU.  Mirrors the sizes
+ * tiny-cuda-nn reports through n_params() / padded_output_width() / level_params_offset().
+ */
+NLOD_API int nlod_layout_json(const char* encoding_json, const char* network_json, uint32_t n_input_dims,
+                              uint32_t n_output_dims, char** json_out);
+
+/* Frees every resource of the module (synchronises the device first). */
+NLOD_API void nlod_module_destroy(nlod_module* m);
+
+/* Sizes: n_params() (network_with_input_encoding.h / object.h), the padded encoding width
+ * fed to the MLP, and the padded output width (16 for the fully fused MLP). */
+NLOD_API size_t   nlod_n_params(const nlod_module* m);
+NLOD_API size_t   nlod_n_network_params(const nlod_module* m);
+NLOD_API uint32_t nlod_n_input_dims(const nlod_module* m);
+NLOD_API uint32_t nlod_n_output_dims(const nlod_module* m);
+NLOD_API uint32_t nlod_encoded_width(const nlod_module* m);
+NLOD_API uint32_t nlod_padded_output_width(const nlod_module* m);
+NLOD_API int      nlod_precision(const nlod_module* m);
+
+/* Per-element maximum grid level, as GridEncoding::set_max_level_gpu
+ * (rptr/ext/tiny-cuda-nn/include/tiny-cuda-nn/encodings/grid.h:916-922, used at :242-265):
+ * device pointer to n floats in [0,1] (fraction of grid levels kept), or NULL to disable.
+ * The pointer is read by every later inference/forward/training call (n elements). */
+NLOD_API int nlod_set_max_level_gpu(nlod_module* m, const float* max_level_gpu);
+/* Scalar maximum level fraction (GridEncoding::set_max_level, grid.h:908-914); default 1000. */
+NLOD_API int nlod_set_max_level(nlod_module* m, float max_level);
+
+/*
+ * Inference with the inference parameters (EMA weights when the optimizer has an EMA
+ * wrapper).  Replaces DifferentiableObject::inference(stream, X, Y)
+ * (rptr/ext/tiny-cuda-nn/include/tiny-cuda-nn/object.h:147-170), called at
+ * rptr/cuda/neural-lod/wavefront_neural_throughput_visibility_lod.cu:595,662.
+ * in: [n][n_input_dims] FP32 device; out: [n][n_output_dims] FP32 device.
+ */
+NLOD_API int nlod_inference(nlod_module* m, void* stream, uint32_t n, const float* in, float* out);
+
+/*
+ * Training-mode forward (training parameters), keeping what backward needs in a context.
+ * Mirrors cpp::Module::forward (cpp_api.h:80).  out may be NULL.  The context is owned by
+ * the caller and freed with nlod_ctx_destroy.
+ */
+NLOD_API int nlod_forward(nlod_module* m, void* stream, uint32_t n, const float* in, float* out, nlod_ctx** ctx);
+
+/*
+ * Backward from dL/d(output) ([n][n_output_dims] FP32 device) into the module's parameter
+ * gradients (overwrite mode, EGradientMode::Overwrite, object.h:115).  Mirrors
+ * cpp::Module::backward (cpp_api.h:81).  `in` must be the input given to nlod_forward.
+ */
+NLOD_API int nlod_backward(nlod_module* m, void* stream, nlod_ctx* ctx, const float* in, const float* dL_dout);
+NLOD_API void nlod_ctx_destroy(nlod_ctx* ctx);
+
+/*
+ * One training step: forward + loss + backward (graph-captured in the reference) + optimizer
+ * step.  Replaces Trainer::training_step(stream, X, Y) (trainer.h:161-186) followed by
+ * Trainer::loss (trainer.h:197-199), called at rptr/cuda/neural-lod/neural_lod_learning.cu:590,686.
+ * target: [n][n_output_dims] FP32 device.  loss_out: NULL or a device float receiving the
+ * mean loss of this step (no host synchronisation).  Loss scale 128 (trainer.h:171).
+ */
+NLOD_API int nlod_training_step(nlod_module* m, void* stream, uint32_t n, const float* in,
+                       const float* target, float* loss_out);
+
+/* Same as nlod_training_step without the optimizer step (run_optimizer = false). */
+NLOD_API int nlod_forward_backward_loss(nlod_module* m, void* stream, uint32_t n, const float* in,
+                               const float* target, float* loss_out);
+
+/* Optimizer step over the current gradients (Trainer::optimizer_step, trainer.h:151-153). */
+NLOD_API int nlod_optimizer_step(nlod_module* m, void* stream);
+
+/* Optimizer step counter and learning rate (Optimizer::step / learning_rate). */
+NLOD_API uint32_t nlod_optimizer_step_count(const nlod_module* m);
+NLOD_API float    nlod_learning_rate(const nlod_module* m);
+NLOD_API int      nlod_set_learning_rate(nlod_module* m, float lr);
+
+/*
+ * FP32 parameter access.  set replaces Trainer::set_params_full_precision
+ * (trainer.h:234-246): writes the FP32 master weights and refreshes the operand copies
+ * and inference weights.  get copies the FP32 master weights (which = 0), the inference
+ * parameters (which = 1, EMA when enabled) or the last gradients (which = 2, unscaled:
+ * dL/dparam of the mean loss).  device_ptr selects device (1) or host (0) buffers.
+ * Both synchronise the device.
+ */
+NLOD_API int nlod_set_params(nlod_module* m, const float* params, size_t n_params, int device_ptr);
+NLOD_API int nlod_get_params(nlod_module* m, float* params, size_t n_params, int which, int device_ptr);
+
+/*
+ * Checkpoints in tiny-cuda-nn's Trainer::serialize JSON form (trainer.h:267-306):
+ * {"n_params": N, "params_type": "__half"|"float", "params_binary": {"bytes": [...]}}.
+ * nlod_serialize allocates *json_out with malloc; free it with nlod_free_string.
+ * half_precision = 1 writes __half inference params (the reference's format).
+ */
+NLOD_API int  nlod_serialize(nlod_module* m, int half_precision, char** json_out);
+NLOD_API int  nlod_deserialize(nlod_module* m, const char* json);
+NLOD_API void nlod_free_string(char* s);
+
+/* Device status word of the last launch sequence (NLOD_OK or NLOD_ERR_TIMEOUT); synchronises. */
+NLOD_API int nlod_sync_status(nlod_module* m, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NLOD_H */

@@ -1,0 +1,106 @@
+// Host-side launchers of the device kernels.  All launchers are asynchronous on `stream`,
+// validate nothing (the C ABI validates first) and return the cudaError_t of the launch.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "desc.h"
+
+namespace nlod {
+
+// Inputs shared by every forward-style launch.
+struct ForwardArgs {
+    uint32_t n;                       // elements (multiple of 128)
+    const float* in;                  // [n][n_input]
+    const float* params;              // FP32 parameters (network then encoding)
+    const void* weights_op;           // network weights in the operand type (FP16/BF16 forms)
+    const float* max_level_gpu;       // nullable, [n]
+    float max_level;                  // scalar fallback (1000 = off)
+    float* out;                       // nullable, [n][n_output]
+    // training extras (all nullable)
+    float* enc;                       // [n][enc_width] encoded input
+    float* hidden;                    // [n_hidden_layers][n][width] post-activation hidden values
+    float* y;                         // [n][16] post-activation outputs (padded)
+    // fused loss (loss_kind != LOSS_NONE)
+    int32_t loss_kind;
+    const float* target;              // [n][n_output]
+    float loss_scale;
+    float* dz;                        // [n][16] dL/d(pre-activation output) * loss_scale
+    float* loss_partial;              // [gridDim.x] per-block loss sums (mean-normalised)
+};
+
+// Plain FP32 form.
+cudaError_t launch_forward_simt(const ModelDesc& d, const ForwardArgs& a, int n_blocks_hint, cudaStream_t s);
+int forward_simt_blocks(const ModelDesc& d);
+
+// dz -> per-layer deltas + dL/d(encoding) (plain FP32).
+struct BackwardArgs {
+    uint32_t n;
+    const float* params;              // FP32 weights
+    const float* hidden;              // [n_hidden][n][width]
+    const float* dz;                  // [n][16]
+    float* delta;                     // [n_hidden][n][width]: delta of hidden layer l (pre-activation)
+    float* d_enc;                     // [n][enc_width]
+};
+cudaError_t launch_backward_delta_simt(const ModelDesc& d, const BackwardArgs& a, cudaStream_t s);
+
+// dW_l += delta_l^T a_{l-1} for every layer (split over rows, FP32 atomics into grads).
+struct WeightGradArgs {
+    uint32_t n;
+    const float* enc;                 // [n][enc_width]
+    const float* hidden;              // [n_hidden][n][width]
+    const float* delta;               // [n_hidden][n][width]
+    const float* dz;                  // [n][16]
+    float* grads;                     // FP32 gradient vector (network part accumulated)
+};
+cudaError_t launch_weight_grad_simt(const ModelDesc& d, const WeightGradArgs& a, cudaStream_t s);
+
+// Grid-table gradient scatter from dL/d(encoding).
+struct GridBackwardArgs {
+    uint32_t n;
+    const float* in;
+    const float* d_enc;               // [n][enc_width]
+    const float* max_level_gpu;
+    float max_level;
+    float* grads;
+};
+cudaError_t launch_grid_backward(const ModelDesc& d, const GridBackwardArgs& a, cudaStream_t s);
+
+// dz[r][c] = dL_dout[r][c] * act'(y[r][c]) for c < n_output, 0 for the padding columns.
+cudaError_t launch_dz_from_dout(const ModelDesc& d, uint32_t n, const float* dL_dout, const float* y, float* dz, cudaStream_t s);
+
+// Sum of per-block partials into *out (single block).
+cudaError_t launch_reduce_sum(const float* partial, uint32_t n, float* out, float scale, cudaStream_t s);
+
+// FP32 -> operand type copy of the network weights (kind 1 = FP16, 2 = BF16).
+cudaError_t launch_convert_weights(const float* src, void* dst, uint32_t n, int kind, cudaStream_t s);
+
+// Parameter initialisation: uniform(lo, hi) from a counter-based PCG stream.
+cudaError_t launch_init_uniform(float* p, uint32_t n, uint64_t seed, uint64_t stream_id, float lo, float hi, cudaStream_t s);
+
+// Optimizer step over all parameters (Adam + optional EMA), see optim.cu.
+struct AdamStepArgs {
+    uint32_t n_params;
+    uint32_t n_matrix;                // leading matrix (network) parameters
+    AdamParams hp;
+    float learning_rate;              // after exponential decay
+    float loss_scale;
+    float lower_lr_bound, upper_lr_bound;
+    float* params;                    // FP32 master
+    const float* grads;               // FP32, scaled by loss_scale
+    float* m1;
+    float* m2;
+    uint32_t* steps;
+    // EMA (nullable ema)
+    float* ema;
+    float ema_decay, ema_debias_old, ema_debias_new;
+};
+cudaError_t launch_adam_step(const AdamStepArgs& a, cudaStream_t s);
+
+// Tensor-core (tcgen05) forms.  kind 1 = FP16, 2 = BF16.
+bool tc_supported(const ModelDesc& d);
+cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, uint32_t* status, cudaStream_t s);
+
+}  // namespace nlod

@@ -1,0 +1,300 @@
+// Tensor-core form of the fused neural-LoD query: encoding + fully fused MLP on tcgen05.
+//
+// One CTA (8 warps) owns a 128-element tile at a time (persistent grid-stride loop):
+//   1. the tile's input rows are staged in shared memory (one coalesced copy);
+//   2. all 256 threads evaluate (element, encoding part) pairs and write the encoded tile as the
+//      MMA A operand (FP16/BF16, K-major no-swizzle core-matrix layout);
+//   3. per layer, one thread issues K/16 tcgen05.mma (M=128, N=width or 16, FP32 accumulate in
+//      TMEM) and commits them to an mbarrier; after the wait every warp reads its 32-lane TMEM
+//      quarter (tcgen05.ld), applies the activation, converts and writes the next A operand back
+//      into the same shared buffer (the MMA has finished reading it);
+//   4. the 16-wide output layer's epilogue applies the output activation and writes FP32 rows.
+// All weights of the network stay resident in shared memory for the CTA's lifetime; several CTAs
+// per SM overlap one CTA's gather-bound encoding with another's MMA chain.
+//
+// The math is tiny-cuda-nn's FullyFusedMLP forward (rptr/ext/tiny-cuda-nn/src/fully_fused_mlp.cu:499-633)
+// with FP32 instead of FP16 accumulation, fed by the composite encoding of encoding.cuh.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "desc.h"
+#include "encoding.cuh"
+#include "kernels.h"
+#include "tc_common.cuh"
+
+namespace nlod {
+
+namespace {
+
+constexpr int kTcTile = 128;
+constexpr int kTcThreads = 256;
+constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
+
+struct TcLayout {
+    uint32_t w_off[kMaxLayers];   // byte offset of each layer's B operand
+    uint32_t w_bytes;
+    uint32_t a_off;               // A operand tile
+    uint32_t a_bytes;
+    uint32_t in_off;              // staged input rows (FP32)
+    uint32_t in_ld;
+    uint32_t bar_off;
+    uint32_t total;
+    uint32_t tmem_cols;
+};
+
+__host__ __device__ inline uint32_t align_up(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
+
+__host__ __device__ inline TcLayout tc_layout(const ModelDesc& d) {
+    TcLayout L{};
+    uint32_t off = 0;
+    for (uint32_t l = 0; l < d.n_layers; ++l) {
+        L.w_off[l] = off;
+        off += d.layer_in[l] * d.layer_out[l] * 2u;
+        off = align_up(off, 128);
+    }
+    L.w_bytes = off;
+    L.a_off = off;
+    const uint32_t ka = d.enc_width > d.width ? d.enc_width : d.width;
+    L.a_bytes = kTcTile * ka * 2u;
+    off = align_up(off + L.a_bytes, 128);
+    L.in_off = off;
+    L.in_ld = d.n_input + 1;
+    off = align_up(off + kTcTile * L.in_ld * 4u, 16);
+    L.bar_off = off;
+    off += 16;   // mbarrier (8) + TMEM base address (4) + timeout flag (4)
+    L.total = align_up(off, 128);
+    L.tmem_cols = d.width + 16 <= 128 ? 128u : 256u;
+    return L;
+}
+
+__device__ __forceinline__ float act_fwd(int32_t act, float v) {
+    switch (act) {
+        case ACT_RELU: return v > 0.f ? v : 0.f;
+        case ACT_SIGMOID: return 1.0f / (1.0f + expf(-v));
+        case ACT_EXP: return expf(v);
+        default: return v;
+    }
+}
+
+template <int W, typename T>
+__global__ void __launch_bounds__(kTcThreads) k_forward_tc(const __grid_constant__ ModelDesc d, const __grid_constant__ ForwardArgs a,
+                                                           uint32_t* __restrict__ status) {
+    using Op = tc::OpType<T>;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const TcLayout L = tc_layout(d);
+    uint8_t* a_tile = smem + L.a_off;
+    float* in_s = reinterpret_cast<float*>(smem + L.in_off);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L.bar_off);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 8);
+
+    const uint32_t tid = threadIdx.x;
+    const uint32_t warp = tid >> 5, lane = tid & 31;
+
+    // ---- set-up: barrier, TMEM, resident weights ----
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        tc::fence_barrier_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tmem_slot, L.tmem_cols);
+        tc::tmem_relinquish();
+    }
+    {
+        // weights_op holds every layer as row-major [out][in] operand-typed values.
+        const uint16_t* wsrc = reinterpret_cast<const uint16_t*>(a.weights_op);
+        for (uint32_t l = 0; l < d.n_layers; ++l) {
+            const uint32_t K = d.layer_in[l], N = d.layer_out[l];
+            const uint32_t sbo = K * 16u;
+            const uint32_t chunks = N * (K / 8u);
+            const uint4* src = reinterpret_cast<const uint4*>(wsrc + d.layer_offset[l]);
+            for (uint32_t c = tid; c < chunks; c += kTcThreads) {
+                const uint32_t n = c / (K / 8u), k0 = (c - n * (K / 8u)) * 8u;
+                *reinterpret_cast<uint4*>(smem + L.w_off[l] + tc::kmajor_offset(n, k0, sbo)) = src[c];
+            }
+        }
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem_base = *tmem_slot;
+    const uint32_t a_addr = tc::smem_addr(a_tile);
+
+    uint32_t phase = 0;
+    bool aborted = false;
+    const uint32_t n_tiles = a.n / kTcTile;
+    const uint32_t quarter = warp & 3u, half = warp >> 2;
+    const uint32_t row = quarter * 32u + lane;   // TMEM lane == tile row owned in the epilogue
+
+    for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const uint32_t row0 = tile * kTcTile;
+        // 1. stage inputs
+        const float* in_tile = a.in + (size_t)row0 * d.n_input;
+        for (uint32_t idx = tid; idx < kTcTile * d.n_input; idx += kTcThreads) {
+            const uint32_t r = idx / d.n_input, c = idx - r * d.n_input;
+            in_s[r * L.in_ld + c] = in_tile[idx];
+        }
+        __syncthreads();
+        // 2. encoding into the A operand (K = enc_width)
+        {
+            const uint32_t sbo = d.enc_width * 16u;
+            for (uint32_t u = tid; u < kTcTile * d.n_parts; u += kTcThreads) {
+                const uint32_t r = u % kTcTile, part = u / kTcTile;
+                const float ml = a.max_level_gpu ? a.max_level_gpu[row0 + r] : a.max_level;
+                encode_part(d, a.params, d.part_slot[part], d.part_level[part], in_s + r * L.in_ld, ml,
+                            [&](uint32_t col, float v) {
+                                *reinterpret_cast<uint16_t*>(a_tile + tc::kmajor_offset(r, col, sbo)) = Op::pack1(v);
+                            });
+            }
+        }
+        tc::fence_proxy_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+
+        // 3. layer chain
+        for (uint32_t l = 0; l < d.n_layers; ++l) {
+            const bool last = l + 1 == d.n_layers;
+            const uint32_t K = d.layer_in[l];
+            const uint32_t N = d.layer_out[l];
+            const uint32_t sbo = K * 16u;
+            const uint32_t d_col = last ? (uint32_t)W : 0u;
+            if (tid == 0) {
+                tc::fence_after_sync();
+                const uint32_t idesc = tc::make_idesc_f16(Op::kFmt, kTcTile, N);
+                const uint32_t b_addr = tc::smem_addr(smem + L.w_off[l]);
+                for (uint32_t k = 0; k < K; k += 16) {
+                    const uint64_t adesc = tc::make_smem_desc(a_addr + (k / 8u) * 128u, 128u, sbo);
+                    const uint64_t bdesc = tc::make_smem_desc(b_addr + (k / 8u) * 128u, 128u, sbo);
+                    tc::mma_f16_ss(tmem_base + d_col, adesc, bdesc, idesc, k > 0 ? 1u : 0u);
+                }
+                tc::mma_commit(bar);
+            }
+            const bool ok = tc::mbar_wait_bounded(bar, phase, kWaitCycles);
+            phase ^= 1u;
+            // Uniform decision: every thread has finished its own bounded wait here.
+            if (__syncthreads_or(!ok)) { aborted = true; break; }
+            tc::fence_after_sync();
+
+            const uint32_t taddr_row = tmem_base + ((quarter * 32u) << 16);
+            if (!last) {
+                // hidden epilogue: warp (quarter, half) converts columns [half*W/2, (half+1)*W/2)
+                const uint32_t out_sbo = (uint32_t)W * 16u;
+#pragma unroll
+                for (uint32_t c0 = 0; c0 < (uint32_t)W / 2u; c0 += 32) {
+                    const uint32_t col = half * ((uint32_t)W / 2u) + c0;
+                    uint32_t r[32];
+                    tc::tmem_ld32(taddr_row + col, r);
+                    tc::tmem_wait_ld();
+#pragma unroll
+                    for (uint32_t j = 0; j < 4; ++j) {
+                        uint4 pk;
+                        pk.x = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * j + 0])), act_fwd(d.act, __uint_as_float(r[8 * j + 1])));
+                        pk.y = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * j + 2])), act_fwd(d.act, __uint_as_float(r[8 * j + 3])));
+                        pk.z = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * j + 4])), act_fwd(d.act, __uint_as_float(r[8 * j + 5])));
+                        pk.w = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * j + 6])), act_fwd(d.act, __uint_as_float(r[8 * j + 7])));
+                        *reinterpret_cast<uint4*>(a_tile + tc::kmajor_offset(row, col + 8u * j, out_sbo)) = pk;
+                    }
+                }
+                tc::fence_proxy_async_smem();
+            } else if (half == 0) {
+                uint32_t r[16];
+                tc::tmem_ld16(taddr_row + d_col, r);
+                tc::tmem_wait_ld();
+                const size_t grow = (size_t)row0 + row;
+                if (a.out) {
+                    for (uint32_t c = 0; c < d.n_output; ++c)
+                        a.out[grow * d.n_output + c] = act_fwd(d.out_act, __uint_as_float(r[c]));
+                }
+                if (a.y) {
+                    float4* yv = reinterpret_cast<float4*>(a.y + grow * 16);
+#pragma unroll
+                    for (uint32_t j = 0; j < 4; ++j)
+                        yv[j] = make_float4(act_fwd(d.out_act, __uint_as_float(r[4 * j])), act_fwd(d.out_act, __uint_as_float(r[4 * j + 1])),
+                                            act_fwd(d.out_act, __uint_as_float(r[4 * j + 2])), act_fwd(d.out_act, __uint_as_float(r[4 * j + 3])));
+                }
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+        }
+        if (aborted) break;
+    }
+
+    // ---- teardown ----
+    if (aborted) {
+        // Give the outstanding MMAs one more bounded chance to finish before TMEM is released.
+        (void)tc::mbar_wait_bounded(bar, phase ^ 1u, kWaitCycles);
+        if (tid == 0) atomicOr(status, 1u);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem_base, L.tmem_cols);
+    }
+}
+
+int g_sms = 0;
+int sm_count() {
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 1;
+    }
+    return g_sms;
+}
+
+// Dynamic shared memory request: what the tile needs, raised so that TMEM (512 columns per SM)
+// can never be over-subscribed by co-resident CTAs.
+size_t tc_smem_bytes(const ModelDesc& d, int* per_sm_out) {
+    const TcLayout L = tc_layout(d);
+    const uint32_t cap = 512u / L.tmem_cols;               // CTAs whose TMEM fits on one SM
+    const size_t sm_bytes = 233472;                        // 228 KB per SM
+    size_t bytes = L.total;
+    // With 1 KB reserved per CTA, at most floor(sm_bytes / (bytes + 1024)) CTAs fit.
+    const size_t min_bytes = sm_bytes / (cap + 1) - 1024 + 16;
+    if (bytes < min_bytes) bytes = min_bytes;
+    bytes = (bytes + 127) / 128 * 128;
+    int per_sm = (int)(sm_bytes / (bytes + 1024));
+    if (per_sm > (int)cap) per_sm = (int)cap;
+    if (per_sm_out) *per_sm_out = per_sm;
+    return bytes;
+}
+
+}  // namespace
+
+bool tc_supported(const ModelDesc& d) {
+    if (d.width != 64 && d.width != 128) return false;
+    if (d.enc_width % 16 != 0 || d.enc_width > 256) return false;
+    int per_sm = 0;
+    const size_t bytes = tc_smem_bytes(d, &per_sm);
+    return bytes <= 227u * 1024u && per_sm >= 1;
+}
+
+cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, uint32_t* status, cudaStream_t s) {
+    int per_sm = 1;
+    const size_t bytes = tc_smem_bytes(d, &per_sm);
+    const uint32_t n_tiles = a.n / kTcTile;
+    uint32_t blocks = (uint32_t)(per_sm * sm_count());
+    if (blocks > n_tiles) blocks = n_tiles;
+    if (blocks == 0) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+#define NLOD_TC_CASE(WD, TY)                                                                          \
+    do {                                                                                              \
+        e = cudaFuncSetAttribute(k_forward_tc<WD, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes); \
+        if (e != cudaSuccess) return e;                                                               \
+        k_forward_tc<WD, TY><<<blocks, kTcThreads, bytes, s>>>(d, a, status);                         \
+    } while (0)
+    if (d.width == 64 && kind == 1) NLOD_TC_CASE(64, __half);
+    else if (d.width == 64 && kind == 2) NLOD_TC_CASE(64, __nv_bfloat16);
+    else if (d.width == 128 && kind == 1) NLOD_TC_CASE(128, __half);
+    else if (d.width == 128 && kind == 2) NLOD_TC_CASE(128, __nv_bfloat16);
+    else return cudaErrorInvalidValue;
+#undef NLOD_TC_CASE
+    return cudaGetLastError();
+}
+
+}  // namespace nlod

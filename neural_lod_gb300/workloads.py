@@ -1,0 +1,121 @@
+"""Network configurations and seeded synthetic inputs of the neural-LoD workloads.
+
+Configurations are tiny-cuda-nn style JSON (the form neural_lod builds in
+rptr/cuda/neural-lod/neural_lod_learning_init.cu:577-676, 822-911), sized as:
+
+  visibility_query   position U[0,1]^3 + direction on S^2 (fed as (d+1)/2) + LoD in {0..7}
+                     applied as a per-element grid max-level (GridEncoding::set_max_level_gpu);
+                     8-level hash grid (F=2, 2^16 entries/level, base 16, scale 1.5) + SH degree 4;
+                     MLP 32 -> 64 -> 64 -> 1 (sigmoid); batch 65,536.
+  throughput_query   position + wi + wo + LoD one-hot over 8; 16-level hash grid (2^19 entries),
+                     SH degree 4 for each direction; MLP 72 (padded to 80) -> 4 x 64 -> 3 (exp);
+                     batch 2^21.
+  visibility_train   visibility_query's architecture with 16 levels (input 48), BCE loss,
+                     Adam lr 1e-2, beta 0.9/0.99, eps 1e-15; batch 2^18.
+Inputs are generated from one uint64 seed with numpy's PCG64 so every run and the oracle see
+identical data.  These seeded synthetic inputs stand in for the paper's scenes, which are not
+available.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def visibility_configs(n_levels: int = 8, log2T: int = 16):
+    encoding = {
+        "otype": "Composite",
+        "nested": [
+            {"otype": "HashGrid", "n_dims_to_encode": 3, "n_levels": n_levels, "n_features_per_level": 2,
+             "log2_hashmap_size": log2T, "base_resolution": 16, "per_level_scale": 1.5},
+            {"otype": "SphericalHarmonics", "n_dims_to_encode": 3, "degree": 4},
+        ],
+    }
+    network = {"otype": "FullyFusedMLP", "n_neurons": 64, "n_hidden_layers": 2, "activation": "ReLU",
+               "output_activation": "Sigmoid"}
+    return encoding, network
+
+
+def throughput_configs():
+    encoding = {
+        "otype": "Composite",
+        "nested": [
+            {"otype": "HashGrid", "n_dims_to_encode": 3, "n_levels": 16, "n_features_per_level": 2,
+             "log2_hashmap_size": 19, "base_resolution": 16, "per_level_scale": 1.5},
+            {"otype": "SphericalHarmonics", "n_dims_to_encode": 3, "degree": 4},
+            {"otype": "SphericalHarmonics", "n_dims_to_encode": 3, "degree": 4},
+            {"otype": "OneHot", "n_dims_to_encode": 1, "n_bins": 8},
+        ],
+    }
+    network = {"otype": "FullyFusedMLP", "n_neurons": 64, "n_hidden_layers": 4, "activation": "ReLU",
+               "output_activation": "Exponential"}
+    return encoding, network
+
+
+VISIBILITY_LOSS = {"otype": "BinaryCrossEntropy"}
+VISIBILITY_OPTIMIZER = {"otype": "Adam", "learning_rate": 1e-2, "beta1": 0.9, "beta2": 0.99, "epsilon": 1e-15,
+                        "l2_reg": 1e-8}
+THROUGHPUT_LOSS = {"otype": "RelativeL2"}
+THROUGHPUT_OPTIMIZER = {"otype": "Ema", "decay": 0.95, "nested": {
+    "otype": "ExponentialDecay", "decay_start": 8000, "decay_interval": 4000, "decay_base": 0.33,
+    "nested": {"otype": "Adam", "learning_rate": 5e-3, "beta1": 0.9, "beta2": 0.99, "epsilon": 1e-15,
+               "l2_reg": 1e-8}}}
+
+WORKLOADS = {
+    "visibility_query": {"batch": 65536, "n_input": 6, "n_output": 1},
+    "throughput_query": {"batch": 1 << 21, "n_input": 10, "n_output": 3},
+    "visibility_train": {"batch": 1 << 18, "n_input": 6, "n_output": 1},
+}
+
+
+def _unit_dirs(rng: np.random.Generator, n: int) -> np.ndarray:
+    v = rng.standard_normal((n, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    return v
+
+
+def visibility_inputs(n: int, seed: int = 0, n_grid_levels: int = 8):
+    """Returns (x [n,6] float32, lod [n] int32, max_level_frac [n] float32).
+
+    LoD k keeps grid levels 0..(n_grid_levels-1-k): fraction (n_grid_levels-1-k)/n_grid_levels.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pos = rng.random((n, 3))
+    d = _unit_dirs(rng, n)
+    lod = rng.integers(0, 8, size=n).astype(np.int32)
+    x = np.concatenate([pos, (d + 1.0) * 0.5], axis=1).astype(np.float32)
+    frac = (np.float32(n_grid_levels - 1) - lod.astype(np.float32)).clip(0) / np.float32(n_grid_levels)
+    return x, lod, frac.astype(np.float32)
+
+
+def throughput_inputs(n: int, seed: int = 1):
+    """Returns x [n,10] float32: position, (wi+1)/2, (wo+1)/2, (lod + 0.5)/8."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pos = rng.random((n, 3))
+    wi = _unit_dirs(rng, n)
+    wo = _unit_dirs(rng, n)
+    lod = rng.integers(0, 8, size=n)
+    x = np.concatenate([pos, (wi + 1.0) * 0.5, (wo + 1.0) * 0.5, ((lod + 0.5) / 8.0)[:, None]], axis=1)
+    return x.astype(np.float32)
+
+
+def xavier_params(spec: dict, seed: int = 7) -> np.ndarray:
+    """FP32 parameter vector for a layout spec: Xavier-uniform matrices (gpu_matrix.h:291-306),
+    grid entries U[-1e-4, 1e-4] (grid.h:1353-1356), scaled up by `grid_gain` for test signal."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    p = np.empty(spec["n_params"], dtype=np.float32)
+    for l in spec["layers"]:
+        s = np.sqrt(6.0 / (l["in"] + l["out"]))
+        p[l["offset"]:l["offset"] + l["in"] * l["out"]] = rng.uniform(-s, s, l["in"] * l["out"])
+    n_net = spec["n_params_network"]
+    p[n_net:] = rng.uniform(-1e-4, 1e-4, spec["n_params"] - n_net)
+    return p
+
+
+def test_params(spec: dict, seed: int = 7, grid_scale: float = 0.5) -> np.ndarray:
+    """Like xavier_params but with grid entries U[-grid_scale, grid_scale], so the grid features
+    carry signal through the MLP (used by the parity tests)."""
+    p = xavier_params(spec, seed)
+    rng = np.random.Generator(np.random.PCG64(seed + 1))
+    n_net = spec["n_params_network"]
+    p[n_net:] = rng.uniform(-grid_scale, grid_scale, spec["n_params"] - n_net)
+    return p

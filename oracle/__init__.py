@@ -1,0 +1,174 @@
+"""CPU oracle of the neural-LoD hot path -- TEST INFRASTRUCTURE ONLY.
+
+Imported only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs, as the
+checker; the product path (libnlod.so and neural_lod_gb300) never imports it.
+The numerics live in nlod_oracle.c (FP64 restatement of tiny-cuda-nn's algorithms, citations in
+nlod_oracle.h); this module builds it, fills its model description from oracle.layout and
+exposes numpy-level helpers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .build import build_oracle
+from .layout import grid_levels, model_spec
+
+ORC_MAX_SLOTS, ORC_MAX_GRIDS, ORC_MAX_LEVELS, ORC_MAX_LAYERS = 8, 2, 32, 10
+LOSS = {"BinaryCrossEntropy": 1, "RelativeL2": 2, "L2": 3}
+
+
+class OrcGrid(C.Structure):
+    _fields_ = [("n_levels", C.c_int32), ("hash", C.c_int32), ("kind", C.c_int32), ("interp", C.c_int32),
+                ("param_offset", C.c_int64), ("offset", C.c_uint32 * (ORC_MAX_LEVELS + 1)),
+                ("res", C.c_uint32 * ORC_MAX_LEVELS), ("scale", C.c_float * ORC_MAX_LEVELS)]
+
+
+class OrcSlot(C.Structure):
+    _fields_ = [("type", C.c_int32), ("in_begin", C.c_int32), ("n_in", C.c_int32), ("out_begin", C.c_int32),
+                ("out_width", C.c_int32), ("n_pad", C.c_int32), ("grid", C.c_int32), ("degree", C.c_int32),
+                ("n_bins", C.c_int32), ("scale", C.c_float), ("offset", C.c_float)]
+
+
+class OrcModel(C.Structure):
+    _fields_ = [("n_input", C.c_int32), ("n_output", C.c_int32), ("enc_width", C.c_int32), ("width", C.c_int32),
+                ("n_layers", C.c_int32), ("act", C.c_int32), ("out_act", C.c_int32),
+                ("layer_in", C.c_int32 * ORC_MAX_LAYERS), ("layer_out", C.c_int32 * ORC_MAX_LAYERS),
+                ("layer_offset", C.c_int64 * ORC_MAX_LAYERS), ("n_slots", C.c_int32), ("n_grids", C.c_int32),
+                ("slots", OrcSlot * ORC_MAX_SLOTS), ("grids", OrcGrid * ORC_MAX_GRIDS),
+                ("n_params", C.c_int64), ("n_params_network", C.c_int64)]
+
+
+class OrcAdam(C.Structure):
+    _fields_ = [(k, C.c_float) for k in ("lr", "beta1", "beta2", "eps", "l2_reg", "rel_decay", "abs_decay", "clip",
+                                         "non_matrix_lr_factor")] + \
+               [("optimize_matrix", C.c_int32), ("optimize_non_matrix", C.c_int32),
+                ("lower_lr_bound", C.c_float), ("upper_lr_bound", C.c_float), ("loss_scale", C.c_float)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(str(build_oracle()))
+        _lib.orc_grid_offsets.restype = C.c_uint32
+        _lib.orc_forward_f32.restype = C.c_int
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class Oracle:
+    """FP64 oracle for one network-with-input-encoding configuration."""
+
+    def __init__(self, encoding: dict, network: dict, n_input: int, n_output: int):
+        self.spec = model_spec(encoding, network, n_input, n_output)
+        s = self.spec
+        m = OrcModel()
+        m.n_input, m.n_output, m.enc_width, m.width = s["n_input"], s["n_output"], s["enc_width"], s["width"]
+        m.n_layers, m.act, m.out_act = s["n_layers"], s["act"], s["out_act"]
+        for i, l in enumerate(s["layers"]):
+            m.layer_in[i], m.layer_out[i], m.layer_offset[i] = l["in"], l["out"], l["offset"]
+        m.n_slots, m.n_grids = len(s["slots"]), len(s["grids"])
+        for i, sl in enumerate(s["slots"]):
+            o = m.slots[i]
+            for k in ("type", "in_begin", "n_in", "out_begin", "out_width", "n_pad", "grid", "degree", "n_bins"):
+                setattr(o, k, sl[k])
+            o.scale, o.offset = sl["scale"], sl["offset"]
+        for i, g in enumerate(s["grids"]):
+            o = m.grids[i]
+            o.n_levels, o.hash, o.kind, o.interp, o.param_offset = g["n_levels"], g["hash"], g["kind"], g["interp"], g["param_offset"]
+            for j, v in enumerate(g["offset"]):
+                o.offset[j] = v
+            for j in range(g["n_levels"]):
+                o.res[j] = g["res"][j]
+                o.scale[j] = g["scale"][j]
+        m.n_params, m.n_params_network = s["n_params"], s["n_params_network"]
+        self.m = m
+        self.n_params = s["n_params"]
+        self.n_output = n_output
+        self.n_input = n_input
+
+    @staticmethod
+    def _in(x):
+        return np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+
+    def encode(self, x, params, max_level=None, max_level_scalar=1000.0):
+        x = self._in(x)
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        ml = None if max_level is None else self._in(max_level)
+        out = np.empty((x.shape[0], self.spec["enc_width"]), dtype=np.float64)
+        lib().orc_encode(C.byref(self.m), C.c_int64(x.shape[0]), _p(x), _p(p), _p(ml), C.c_float(max_level_scalar), _p(out))
+        return out
+
+    def forward(self, x, params, max_level=None, max_level_scalar=1000.0, with_y16=False):
+        x = self._in(x)
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        ml = None if max_level is None else self._in(max_level)
+        out = np.empty((x.shape[0], self.n_output), dtype=np.float64)
+        y16 = np.empty((x.shape[0], 16), dtype=np.float64) if with_y16 else None
+        lib().orc_forward(C.byref(self.m), C.c_int64(x.shape[0]), _p(x), _p(p), _p(ml), C.c_float(max_level_scalar), _p(out), _p(y16))
+        return (out, y16) if with_y16 else out
+
+    def loss(self, loss_name, y16, target, loss_scale=1.0):
+        y16 = np.ascontiguousarray(y16, dtype=np.float64)
+        t = self._in(target)
+        dz = np.empty_like(y16)
+        val = C.c_double()
+        lib().orc_loss(C.byref(self.m), LOSS[loss_name], C.c_int64(y16.shape[0]), _p(y16), _p(t), C.c_double(loss_scale),
+                       C.byref(val), _p(dz))
+        return val.value, dz
+
+    def backward(self, x, params, dz16, max_level=None, max_level_scalar=1000.0):
+        x = self._in(x)
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        ml = None if max_level is None else self._in(max_level)
+        dz = np.ascontiguousarray(dz16, dtype=np.float64)
+        g = np.zeros(self.n_params, dtype=np.float64)
+        lib().orc_backward(C.byref(self.m), C.c_int64(x.shape[0]), _p(x), _p(p), _p(ml), C.c_float(max_level_scalar), _p(dz), _p(g))
+        return g
+
+    def loss_and_grad(self, loss_name, x, params, target, max_level=None, loss_scale=1.0):
+        _, y16 = self.forward(x, params, max_level=max_level, with_y16=True)
+        val, dz = self.loss(loss_name, y16, target, loss_scale)
+        return val, self.backward(x, params, dz, max_level=max_level)
+
+    def forward_f32(self, x, params, max_level=None, max_level_scalar=1000.0, n_threads=0):
+        """FP32 scalar host forward (the timed CPU baseline); returns (out, threads_used)."""
+        x = self._in(x)
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        ml = None if max_level is None else self._in(max_level)
+        out = np.empty((x.shape[0], self.n_output), dtype=np.float32)
+        used = lib().orc_forward_f32(C.byref(self.m), C.c_int64(x.shape[0]), _p(x), _p(p), _p(ml), C.c_float(max_level_scalar),
+                                     _p(out), C.c_int(n_threads))
+        return out, used
+
+
+def adam_step(hp: dict, params, grads, m1, m2, steps, n_matrix, loss_scale=1.0, ema=None, ema_decay=0.0,
+              ema_debias_old=0.0, ema_debias_new=1.0, lower=0.0, upper=3.4e38):
+    """In-place FP32 Adam step (adam.h:47-119) on numpy arrays."""
+    a = OrcAdam()
+    a.lr = hp.get("learning_rate", 1e-3)
+    a.beta1, a.beta2, a.eps = hp.get("beta1", 0.9), hp.get("beta2", 0.999), hp.get("epsilon", 1e-8)
+    a.l2_reg = hp.get("l2_reg", 1e-8)
+    a.rel_decay, a.abs_decay = hp.get("relative_decay", 0.0), hp.get("absolute_decay", 0.0)
+    a.clip = hp.get("clipping_magnitude", 0.0)
+    a.non_matrix_lr_factor = hp.get("non_matrix_learning_rate_factor", 1.0)
+    a.optimize_matrix, a.optimize_non_matrix = 1, 1
+    a.lower_lr_bound, a.upper_lr_bound, a.loss_scale = lower, upper, loss_scale
+    lib().orc_adam_step(C.byref(a), C.c_int64(params.size), C.c_int64(n_matrix), _p(params), _p(grads), _p(m1), _p(m2),
+                        _p(steps), _p(ema), C.c_float(ema_decay), C.c_float(ema_debias_old), C.c_float(ema_debias_new))
+
+
+def sh(degree: int, x: float, y: float, z: float):
+    out = (C.c_double * (degree * degree))()
+    lib().orc_sh(C.c_int(degree), C.c_double(x), C.c_double(y), C.c_double(z), out)
+    return np.array(out[:], dtype=np.float64)
+
+
+__all__ = ["Oracle", "adam_step", "sh", "grid_levels", "model_spec"]

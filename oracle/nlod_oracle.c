@@ -1,0 +1,475 @@
+/*
+ * CPU oracle of the neural-LoD hot path -- TEST INFRASTRUCTURE ONLY (see nlod_oracle.h).
+ * Build: oracle/build.py (gcc -O2 -ffp-contract=off -fopenmp -shared).
+ */
+#include "nlod_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ---------------------------------------------------------------------------------------------
+ * Grid layout: grid.h:195-204 (scale/resolution) and 982-1015 (offset table).
+ * ------------------------------------------------------------------------------------------- */
+uint32_t orc_grid_offsets(int n_levels, uint32_t log2_hashmap_size, uint32_t base_resolution, float per_level_scale,
+                          int kind, uint32_t* offsets, uint32_t* res, float* scale) {
+    const float log2s = log2f(per_level_scale);
+    uint32_t off = 0;
+    for (int i = 0; i < n_levels; ++i) {
+        const float s = exp2f((float)i * log2s) * (float)base_resolution - 1.0f;
+        const uint32_t r = (uint32_t)ceilf(s) + 1u;
+        const uint32_t max_params = 0xFFFFFFFFu / 2u;
+        uint32_t p;
+        if (powf((float)r, 3.0f) > (float)max_params) p = max_params;
+        else p = r * r * r;
+        p = (p + 7u) / 8u * 8u;
+        if (kind == 2) {
+            uint32_t t = base_resolution * base_resolution * base_resolution;
+            if (t < p) p = t;
+        } else if (kind == 0) {
+            uint32_t t = 1u << log2_hashmap_size;
+            if (t < p) p = t;
+        }
+        offsets[i] = off;
+        if (res) res[i] = r;
+        if (scale) scale[i] = s;
+        off += p;
+    }
+    offsets[n_levels] = off;
+    return off;
+}
+
+/* grid.h:111-187 */
+static uint32_t orc_hash(int kind, uint32_t x, uint32_t y, uint32_t z) {
+    if (kind == 0) return (x * 1u) ^ (y * 2654435761u) ^ (z * 805459861u);
+    if (kind == 1) return (x * 1958374283u) ^ (y * 2654435761u) ^ (z * 805459861u);
+    return (x * 2165219737u) ^ (y * 1434869437u) ^ (z * 2097192037u);
+}
+
+static uint32_t orc_grid_index(const OrcGrid* g, int level, const uint32_t pos[3]) {
+    const uint32_t size = g->offset[level + 1] - g->offset[level];
+    uint32_t stride = 1, index = 0;
+    for (int dim = 0; dim < 3 && stride <= size; ++dim) {
+        index += pos[dim] * stride;
+        stride *= g->res[level];
+    }
+    if (g->kind == 0 && size < stride) index = orc_hash(g->hash, pos[0], pos[1], pos[2]);
+    return index % size;
+}
+
+/* common_device.h:437-464 with FP32 arithmetic: p = x*scale + 0.5 (fused), cell = floor(p). */
+static void orc_pos_fract(float x, float scale, float* frac, uint32_t* cell) {
+    const float p = fmaf(x, scale, 0.5f);
+    const float fl = floorf(p);
+    *cell = (uint32_t)(int)fl;
+    *frac = p - fl;
+}
+
+static double orc_interp(int interp, double t) { return interp == 2 ? t * t * (3.0 - 2.0 * t) : t; }
+
+static int orc_masked_fwd(int level, float ml_frac, int n_levels) {
+    const float max_level = (ml_frac * (float)(n_levels * 2)) / 2.0f;
+    return (float)level >= max_level + 1e-3f;
+}
+static int orc_skipped_bwd(int level, float ml_frac, int n_levels) {
+    const float max_level = (ml_frac * (float)(n_levels * 2)) / 2.0f;
+    return (float)level > max_level + 1e-3f;
+}
+
+/* Corner entries (table indices within the level) and weights of one level. Returns corners. */
+static int orc_corners(const OrcGrid* g, int level, const float p[3], uint32_t entries[8], double weights[8]) {
+    float frac[3];
+    uint32_t cell[3];
+    for (int d = 0; d < 3; ++d) orc_pos_fract(p[d], g->scale[level], &frac[d], &cell[d]);
+    if (g->interp == 1) {
+        entries[0] = orc_grid_index(g, level, cell);
+        weights[0] = 1.0;
+        return 1;
+    }
+    double t[3];
+    for (int d = 0; d < 3; ++d) t[d] = orc_interp(g->interp, (double)frac[d]);
+    for (int c = 0; c < 8; ++c) {
+        uint32_t q[3];
+        double w = 1.0;
+        for (int d = 0; d < 3; ++d) {
+            if (c & (1 << d)) { w *= t[d]; q[d] = cell[d] + 1u; }
+            else { w *= 1.0 - t[d]; q[d] = cell[d]; }
+        }
+        entries[c] = orc_grid_index(g, level, q);
+        weights[c] = w;
+    }
+    return 8;
+}
+
+/* ---------------------------------------------------------------------------------------------
+ * Spherical harmonics by recurrence: Y_l^m = K_l^m Pbar_l^m(z) * {sqrt2 Re, sqrt2 Im, 1}((x+iy)^|m|)
+ * with Pbar_l^m = P_l^m / sin^m (Condon-Shortley phase included).
+ * ------------------------------------------------------------------------------------------- */
+static double orc_fact(int n) { double r = 1.0; for (int i = 2; i <= n; ++i) r *= i; return r; }
+
+void orc_sh(int degree, double x, double y, double z, double* out) {
+    const double pi = 3.14159265358979323846;
+    double pbar[9][9];
+    memset(pbar, 0, sizeof pbar);
+    for (int m = 0; m < degree; ++m) {
+        double pmm = (m % 2) ? -1.0 : 1.0; /* (-1)^m (2m-1)!! */
+        for (int k = 1; k <= 2 * m - 1; k += 2) pmm *= k;
+        pbar[m][m] = pmm;
+        if (m + 1 < degree) pbar[m + 1][m] = z * (2 * m + 1) * pmm;
+        for (int l = m + 2; l < degree; ++l)
+            pbar[l][m] = ((2 * l - 1) * z * pbar[l - 1][m] - (l + m - 1) * pbar[l - 2][m]) / (l - m);
+    }
+    double re[9], im[9];
+    re[0] = 1.0; im[0] = 0.0;
+    for (int m = 1; m < 9; ++m) {
+        re[m] = re[m - 1] * x - im[m - 1] * y;
+        im[m] = re[m - 1] * y + im[m - 1] * x;
+    }
+    for (int l = 0; l < degree; ++l) {
+        for (int m = -l; m <= l; ++m) {
+            const int am = m < 0 ? -m : m;
+            const double K = sqrt((2.0 * l + 1.0) / (4.0 * pi) * orc_fact(l - am) / orc_fact(l + am));
+            double v;
+            if (m > 0) v = sqrt(2.0) * K * pbar[l][am] * re[am];
+            else if (m < 0) v = sqrt(2.0) * K * pbar[l][am] * im[am];
+            else v = K * pbar[l][0];
+            out[l * l + l + m] = v;
+        }
+    }
+}
+
+/* ---------------------------------------------------------------------------------------------
+ * Encoding (composite concatenation, composite.h:215-281)
+ * ------------------------------------------------------------------------------------------- */
+static void orc_encode_row(const OrcModel* m, const float* row, const double* params, float ml, double* enc) {
+    for (int si = 0; si < m->n_slots; ++si) {
+        const OrcSlot* s = &m->slots[si];
+        double* o = enc + s->out_begin;
+        switch (s->type) {
+            case ORC_GRID: {
+                const OrcGrid* g = &m->grids[s->grid];
+                for (int l = 0; l < g->n_levels; ++l) {
+                    double f0 = 0.0, f1 = 0.0;
+                    if (!orc_masked_fwd(l, ml, g->n_levels)) {
+                        uint32_t e[8];
+                        double w[8];
+                        const int nc = orc_corners(g, l, row + s->in_begin, e, w);
+                        const double* tab = params + g->param_offset + 2 * (int64_t)g->offset[l];
+                        for (int c = 0; c < nc; ++c) {
+                            f0 += w[c] * tab[2 * (int64_t)e[c]];
+                            f1 += w[c] * tab[2 * (int64_t)e[c] + 1];
+                        }
+                    }
+                    o[2 * l] = f0;
+                    o[2 * l + 1] = f1;
+                }
+                for (int p = 0; p < s->n_pad; ++p) o[2 * g->n_levels + p] = 0.0;
+                break;
+            }
+            case ORC_SH: {
+                for (int p = 0; p < s->n_pad; ++p) o[p] = 1.0;
+                const double x = (double)row[s->in_begin] * 2.0 - 1.0;
+                const double y = (double)row[s->in_begin + 1] * 2.0 - 1.0;
+                const double z = (double)row[s->in_begin + 2] * 2.0 - 1.0;
+                orc_sh(s->degree, x, y, z, o + s->n_pad);
+                break;
+            }
+            case ORC_IDENTITY: {
+                for (int j = 0; j < s->n_in; ++j) o[j] = (double)row[s->in_begin + j] * s->scale + s->offset;
+                for (int p = 0; p < s->n_pad; ++p) o[s->n_in + p] = 1.0;
+                break;
+            }
+            case ORC_ONEHOT: {
+                int bin = (int)floorf(row[s->in_begin] * (float)s->n_bins);
+                if (bin < 0) bin = 0;
+                if (bin >= s->n_bins) bin = s->n_bins - 1;
+                for (int j = 0; j < s->n_bins; ++j) o[j] = j == bin ? 1.0 : 0.0;
+                for (int p = 0; p < s->n_pad; ++p) o[s->n_bins + p] = 0.0;
+                break;
+            }
+            default: break;
+        }
+    }
+}
+
+void orc_encode(const OrcModel* m, int64_t n, const float* in, const double* params, const float* max_level,
+                float max_level_scalar, double* enc) {
+    for (int64_t i = 0; i < n; ++i)
+        orc_encode_row(m, in + i * m->n_input, params, max_level ? max_level[i] : max_level_scalar, enc + i * m->enc_width);
+}
+
+/* ---------------------------------------------------------------------------------------------
+ * MLP (fully_fused_mlp.cu): h_{l+1} = act(W_l h_l), output layer padded to 16 rows.
+ * ------------------------------------------------------------------------------------------- */
+static double orc_act(int act, double v) {
+    switch (act) {
+        case ORC_ACT_RELU: return v > 0.0 ? v : 0.0;
+        case ORC_ACT_SIGMOID: return 1.0 / (1.0 + exp(-v));
+        case ORC_ACT_EXP: return exp(v);
+        default: return v;
+    }
+}
+static double orc_act_grad_out(int act, double y) {
+    switch (act) {
+        case ORC_ACT_RELU: return y > 0.0 ? 1.0 : 0.0;
+        case ORC_ACT_SIGMOID: return y * (1.0 - y);
+        case ORC_ACT_EXP: return y;
+        default: return 1.0;
+    }
+}
+
+/* acts: buffer of (n_layers) * 256 doubles: acts[l] = input of layer l (acts[0] = encoding). */
+static void orc_mlp_row(const OrcModel* m, const double* params, const double* enc, double* acts, double* y16) {
+    memcpy(acts, enc, sizeof(double) * m->enc_width);
+    for (int l = 0; l < m->n_layers; ++l) {
+        const double* W = params + m->layer_offset[l];
+        const double* a = acts + 256 * l;
+        const int nin = m->layer_in[l], nout = m->layer_out[l];
+        const int last = l + 1 == m->n_layers;
+        double* o = last ? y16 : acts + 256 * (l + 1);
+        for (int j = 0; j < nout; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < nin; ++k) s += W[(int64_t)j * nin + k] * a[k];
+            o[j] = orc_act(last ? m->out_act : m->act, s);
+        }
+    }
+}
+
+void orc_forward(const OrcModel* m, int64_t n, const float* in, const double* params, const float* max_level,
+                 float max_level_scalar, double* out, double* y16) {
+#pragma omp parallel
+    {
+        double* enc = (double*)malloc(sizeof(double) * 256);
+        double* acts = (double*)malloc(sizeof(double) * 256 * ORC_MAX_LAYERS);
+        double y[16];
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            orc_encode_row(m, in + i * m->n_input, params, max_level ? max_level[i] : max_level_scalar, enc);
+            orc_mlp_row(m, params, enc, acts, y);
+            if (out)
+                for (int c = 0; c < m->n_output; ++c) out[i * m->n_output + c] = y[c];
+            if (y16) memcpy(y16 + i * 16, y, sizeof y);
+        }
+        free(enc);
+        free(acts);
+    }
+}
+
+/* losses/*.h: value / n_total, gradient * loss_scale / n_total, then output activation derivative. */
+void orc_loss(const OrcModel* m, int loss_kind, int64_t n, const double* y16, const float* target, double loss_scale,
+              double* loss, double* dz16) {
+    const double n_total = (double)n * (double)m->n_output;
+    double total = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        for (int c = 0; c < 16; ++c) {
+            double g = 0.0;
+            if (c < m->n_output) {
+                const double y = y16[i * 16 + c];
+                const double t = target[i * m->n_output + c];
+                double v;
+                if (loss_kind == ORC_LOSS_BCE) {
+                    const double eps = (double)1e-5f;
+                    double p = y < eps ? eps : y;
+                    if (p > 1.0 - eps) p = 1.0 - eps;
+                    v = -(t * log(p) + (1.0 - t) * log(1.0 - p));
+                    g = -(t - p) / (p - p * p);
+                } else if (loss_kind == ORC_LOSS_RELL2) {
+                    const double den = y * y + (double)0.01f;
+                    v = (y - t) * (y - t) / den;
+                    g = 2.0 * (y - t) / den;
+                } else {
+                    v = (y - t) * (y - t);
+                    g = 2.0 * (y - t);
+                }
+                total += v / n_total;
+                g = g * loss_scale / n_total * orc_act_grad_out(m->out_act, y);
+            }
+            if (dz16) dz16[i * 16 + c] = g;
+        }
+    }
+    if (loss) *loss = total;
+}
+
+void orc_backward(const OrcModel* m, int64_t n, const float* in, const double* params, const float* max_level,
+                  float max_level_scalar, const double* dz16, double* grads) {
+    double* enc = (double*)malloc(sizeof(double) * 256);
+    double* acts = (double*)malloc(sizeof(double) * 256 * ORC_MAX_LAYERS);
+    double* delta = (double*)malloc(sizeof(double) * 256);
+    double* nd = (double*)malloc(sizeof(double) * 256);
+    double y[16];
+    for (int64_t i = 0; i < n; ++i) {
+        const float* row = in + i * m->n_input;
+        const float ml = max_level ? max_level[i] : max_level_scalar;
+        orc_encode_row(m, row, params, ml, enc);
+        orc_mlp_row(m, params, enc, acts, y);
+        for (int c = 0; c < 16; ++c) delta[c] = dz16[i * 16 + c];
+        for (int l = m->n_layers - 1; l >= 0; --l) {
+            const double* W = params + m->layer_offset[l];
+            double* G = grads + m->layer_offset[l];
+            const double* a = acts + 256 * l;
+            const int nin = m->layer_in[l], nout = m->layer_out[l];
+            for (int o = 0; o < nout; ++o) {
+                if (delta[o] == 0.0) continue;
+                for (int k = 0; k < nin; ++k) G[(int64_t)o * nin + k] += delta[o] * a[k];
+            }
+            for (int k = 0; k < nin; ++k) {
+                double s = 0.0;
+                for (int o = 0; o < nout; ++o) s += delta[o] * W[(int64_t)o * nin + k];
+                if (l > 0) s *= (m->act == ORC_ACT_RELU) ? (a[k] > 0.0 ? 1.0 : 0.0) : 1.0;
+                nd[k] = s;
+            }
+            memcpy(delta, nd, sizeof(double) * nin);
+        }
+        /* delta now holds dL/d(encoding); scatter into grid tables (grid.h:394-517). */
+        for (int si = 0; si < m->n_slots; ++si) {
+            const OrcSlot* s = &m->slots[si];
+            if (s->type != ORC_GRID) continue;
+            const OrcGrid* g = &m->grids[s->grid];
+            for (int l = 0; l < g->n_levels; ++l) {
+                if (orc_skipped_bwd(l, ml, g->n_levels)) continue;
+                uint32_t e[8];
+                double w[8];
+                const int nc = orc_corners(g, l, row + s->in_begin, e, w);
+                double* tab = grads + g->param_offset + 2 * (int64_t)g->offset[l];
+                const double d0 = delta[s->out_begin + 2 * l], d1 = delta[s->out_begin + 2 * l + 1];
+                for (int c = 0; c < nc; ++c) {
+                    tab[2 * (int64_t)e[c]] += w[c] * d0;
+                    tab[2 * (int64_t)e[c] + 1] += w[c] * d1;
+                }
+            }
+        }
+    }
+    free(enc);
+    free(acts);
+    free(delta);
+    free(nd);
+}
+
+/* adam.h:47-119 in FP32, followed by the EMA update of ema.h:45-76 when ema != NULL. */
+void orc_adam_step(const OrcAdam* a, int64_t n_params, int64_t n_matrix, float* params, const float* grads,
+                   float* m1, float* m2, uint32_t* steps, float* ema, float ema_decay, float ema_debias_old,
+                   float ema_debias_new) {
+    for (int64_t i = 0; i < n_params; ++i) {
+        const int matrix = i < n_matrix;
+        float w = params[i];
+        float g = grads[i] / a->loss_scale;
+        int skip = matrix ? !a->optimize_matrix : (!a->optimize_non_matrix || g == 0.0f);
+        if (!skip) {
+            if (matrix) g += a->l2_reg * w;
+            const float g2 = g * g;
+            m1[i] = a->beta1 * m1[i] + (1.0f - a->beta1) * g;
+            m2[i] = a->beta2 * m2[i] + (1.0f - a->beta2) * g2;
+            float lr = a->lr;
+            if (!matrix) lr *= a->non_matrix_lr_factor;
+            const uint32_t step = ++steps[i];
+            lr *= sqrtf(1.0f - powf(a->beta2, (float)step)) / (1.0f - powf(a->beta1, (float)step));
+            float eff = lr / (sqrtf(m2[i]) + a->eps);
+            if (eff < a->lower_lr_bound) eff = a->lower_lr_bound;
+            if (eff > a->upper_lr_bound) eff = a->upper_lr_bound;
+            const float rel = a->rel_decay * lr, absd = a->abs_decay * lr;
+            const float decayed = (1.0f - rel) * w - copysignf(absd, w);
+            float nw = decayed - eff * m1[i];
+            if (a->clip != 0.0f) nw = nw < -a->clip ? -a->clip : (nw > a->clip ? a->clip : nw);
+            params[i] = nw;
+            w = nw;
+        }
+        if (ema) ema[i] = (ema[i] * ema_decay * ema_debias_old + w * (1.0f - ema_decay)) * ema_debias_new;
+    }
+}
+
+/* ---------------------------------------------------------------------------------------------
+ * FP32 scalar forward over all host threads (CPU baseline).
+ * ------------------------------------------------------------------------------------------- */
+static float orc_actf(int act, float v) {
+    switch (act) {
+        case ORC_ACT_RELU: return v > 0.f ? v : 0.f;
+        case ORC_ACT_SIGMOID: return 1.0f / (1.0f + expf(-v));
+        case ORC_ACT_EXP: return expf(v);
+        default: return v;
+    }
+}
+
+int orc_forward_f32(const OrcModel* m, int64_t n, const float* in, const float* params, const float* max_level,
+                    float max_level_scalar, float* out, int n_threads) {
+    int used = 1;
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+#pragma omp parallel
+    {
+#ifdef _OPENMP
+#pragma omp single
+        used = omp_get_num_threads();
+#endif
+        float a[256], b[256];
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            const float* row = in + i * m->n_input;
+            const float ml = max_level ? max_level[i] : max_level_scalar;
+            for (int si = 0; si < m->n_slots; ++si) {
+                const OrcSlot* s = &m->slots[si];
+                float* o = a + s->out_begin;
+                if (s->type == ORC_GRID) {
+                    const OrcGrid* g = &m->grids[s->grid];
+                    for (int l = 0; l < g->n_levels; ++l) {
+                        float f0 = 0.f, f1 = 0.f;
+                        if (!orc_masked_fwd(l, ml, g->n_levels)) {
+                            float frac[3];
+                            uint32_t cell[3];
+                            for (int d = 0; d < 3; ++d) orc_pos_fract(row[s->in_begin + d], g->scale[l], &frac[d], &cell[d]);
+                            const float* tab = params + g->param_offset + 2 * (int64_t)g->offset[l];
+                            for (int c = 0; c < 8; ++c) {
+                                uint32_t q[3];
+                                float w = 1.f;
+                                for (int d = 0; d < 3; ++d) {
+                                    if (c & (1 << d)) { w *= frac[d]; q[d] = cell[d] + 1u; }
+                                    else { w *= 1.f - frac[d]; q[d] = cell[d]; }
+                                }
+                                const uint32_t e = orc_grid_index(g, l, q);
+                                f0 += w * tab[2 * (int64_t)e];
+                                f1 += w * tab[2 * (int64_t)e + 1];
+                            }
+                        }
+                        o[2 * l] = f0;
+                        o[2 * l + 1] = f1;
+                    }
+                    for (int p = 0; p < s->n_pad; ++p) o[2 * g->n_levels + p] = 0.f;
+                } else if (s->type == ORC_SH) {
+                    double tmp[64];
+                    for (int p = 0; p < s->n_pad; ++p) o[p] = 1.f;
+                    orc_sh(s->degree, row[s->in_begin] * 2.f - 1.f, row[s->in_begin + 1] * 2.f - 1.f, row[s->in_begin + 2] * 2.f - 1.f, tmp);
+                    for (int j = 0; j < s->degree * s->degree; ++j) o[s->n_pad + j] = (float)tmp[j];
+                } else if (s->type == ORC_IDENTITY) {
+                    for (int j = 0; j < s->n_in; ++j) o[j] = row[s->in_begin + j] * s->scale + s->offset;
+                    for (int p = 0; p < s->n_pad; ++p) o[s->n_in + p] = 1.f;
+                } else {
+                    int bin = (int)floorf(row[s->in_begin] * (float)s->n_bins);
+                    if (bin < 0) bin = 0;
+                    if (bin >= s->n_bins) bin = s->n_bins - 1;
+                    for (int j = 0; j < s->n_bins; ++j) o[j] = j == bin ? 1.f : 0.f;
+                    for (int p = 0; p < s->n_pad; ++p) o[s->n_bins + p] = 0.f;
+                }
+            }
+            float* cur = a;
+            float* nxt = b;
+            for (int l = 0; l < m->n_layers; ++l) {
+                const float* W = params + m->layer_offset[l];
+                const int nin = m->layer_in[l], nout = m->layer_out[l];
+                const int last = l + 1 == m->n_layers;
+                for (int j = 0; j < nout; ++j) {
+                    float s = 0.f;
+                    for (int k = 0; k < nin; ++k) s += W[(int64_t)j * nin + k] * cur[k];
+                    nxt[j] = orc_actf(last ? m->out_act : m->act, s);
+                }
+                float* t = cur;
+                cur = nxt;
+                nxt = t;
+            }
+            for (int c = 0; c < m->n_output; ++c) out[i * m->n_output + c] = cur[c];
+        }
+    }
+    return used;
+}

@@ -1,0 +1,117 @@
+/*
+ * CPU oracle of the neural-LoD hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline legs may load this
+ * library; the product (libnlod.so) never calls it.  It restates, in plain C, tiny-cuda-nn's
+ * algorithms for the neural_lod network path (paths relative to rptr/ext/tiny-cuda-nn/):
+ *   grid offset table / resolution     include/tiny-cuda-nn/encodings/grid.h:195-204, 982-1015
+ *   grid index + hashes                encodings/grid.h:111-187
+ *   pos_fract                          include/tiny-cuda-nn/common_device.h:437-464
+ *   grid forward / backward            encodings/grid.h:220-392 / 394-517
+ *   spherical harmonics                encodings/spherical_harmonics.h:46-151
+ *   composite concatenation            encodings/composite.h:215-281
+ *   fully fused MLP forward/backward   src/fully_fused_mlp.cu:499-633, 733-833
+ *   losses                             include/tiny-cuda-nn/losses/binary_cross_entropy.h:7-43,
+ *                                      losses/relative_l2.h:39-76, losses/l2.h
+ *   Adam / EMA / exponential decay     optimizers/adam.h:47-188, ema.h:45-124, exponential_decay.h:60-71
+ * The continuous arithmetic is FP64 ("FP64 oracle"); the discrete choices (grid cell of a
+ * position, hash index) are made in FP32 exactly as the GPU makes them, so that both pick the
+ * same table entries.  Spherical harmonics are evaluated by the associated-Legendre recurrence,
+ * independently of the generated polynomials the kernels use.
+ *
+ * Pinning: layout rules and SH values are checked against fixtures generated from the
+ * reference sources (tests/golden/make_golden.py); gradients are checked against FP64 central
+ * finite differences of this oracle's own forward.
+ */
+#ifndef NLOD_ORACLE_H
+#define NLOD_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_MAX_SLOTS 8
+#define ORC_MAX_GRIDS 2
+#define ORC_MAX_LEVELS 32
+#define ORC_MAX_LAYERS 10
+
+enum { ORC_GRID = 0, ORC_SH = 1, ORC_IDENTITY = 2, ORC_ONEHOT = 3 };
+enum { ORC_ACT_NONE = 0, ORC_ACT_RELU = 1, ORC_ACT_SIGMOID = 2, ORC_ACT_EXP = 3 };
+enum { ORC_LOSS_BCE = 1, ORC_LOSS_RELL2 = 2, ORC_LOSS_L2 = 3 };
+
+typedef struct {
+    int32_t n_levels;
+    int32_t hash;      /* 0 coherent prime, 1 prime, 2 reversed prime */
+    int32_t kind;      /* 0 hash, 1 dense, 2 tiled */
+    int32_t interp;    /* 0 linear, 1 nearest, 2 smoothstep */
+    int64_t param_offset;
+    uint32_t offset[ORC_MAX_LEVELS + 1];
+    uint32_t res[ORC_MAX_LEVELS];
+    float scale[ORC_MAX_LEVELS];
+} OrcGrid;
+
+typedef struct {
+    int32_t type;
+    int32_t in_begin, n_in;
+    int32_t out_begin, out_width, n_pad;
+    int32_t grid;
+    int32_t degree, n_bins;
+    float scale, offset;
+} OrcSlot;
+
+typedef struct {
+    int32_t n_input, n_output, enc_width, width, n_layers, act, out_act;
+    int32_t layer_in[ORC_MAX_LAYERS], layer_out[ORC_MAX_LAYERS];
+    int64_t layer_offset[ORC_MAX_LAYERS];
+    int32_t n_slots, n_grids;
+    OrcSlot slots[ORC_MAX_SLOTS];
+    OrcGrid grids[ORC_MAX_GRIDS];
+    int64_t n_params, n_params_network;
+} OrcModel;
+
+/* grid.h:195-204 + 982-1015: per-level scale/resolution and offsets (entries). Returns n entries. */
+uint32_t orc_grid_offsets(int n_levels, uint32_t log2_hashmap_size, uint32_t base_resolution, float per_level_scale,
+                          int kind, uint32_t* offsets /* n_levels+1 */, uint32_t* res, float* scale);
+
+/* Real SH basis (degree^2 values) of direction (x,y,z) in [-1,1]^3 (already mapped), FP64. */
+void orc_sh(int degree, double x, double y, double z, double* out);
+
+/* Encoded rows [n][enc_width], FP64.  max_level: NULL or per-element fractions. */
+void orc_encode(const OrcModel* m, int64_t n, const float* in, const double* params, const float* max_level,
+                float max_level_scalar, double* enc);
+
+/* Forward: out [n][n_output] post-activation; y16 (nullable) [n][16] padded post-activation. */
+void orc_forward(const OrcModel* m, int64_t n, const float* in, const double* params, const float* max_level,
+                 float max_level_scalar, double* out, double* y16);
+
+/* Loss values (mean over n*n_output, summed into *loss) and dz16 = dL/d(pre-activation output)
+ * * loss_scale (padding columns zero). */
+void orc_loss(const OrcModel* m, int loss_kind, int64_t n, const double* y16, const float* target, double loss_scale,
+              double* loss, double* dz16);
+
+/* Parameter gradients from dz16, accumulated into grads[n_params]. */
+void orc_backward(const OrcModel* m, int64_t n, const float* in, const double* params, const float* max_level,
+                  float max_level_scalar, const double* dz16, double* grads);
+
+/* One Adam step (adam.h:47-119) in FP32 on all parameters; m1, m2, steps updated. */
+typedef struct {
+    float lr, beta1, beta2, eps, l2_reg, rel_decay, abs_decay, clip, non_matrix_lr_factor;
+    int32_t optimize_matrix, optimize_non_matrix;
+    float lower_lr_bound, upper_lr_bound;
+    float loss_scale;
+} OrcAdam;
+void orc_adam_step(const OrcAdam* a, int64_t n_params, int64_t n_matrix, float* params, const float* grads,
+                   float* m1, float* m2, uint32_t* steps, float* ema, float ema_decay, float ema_debias_old,
+                   float ema_debias_new);
+
+/* FP32 scalar forward over all host threads: the timed CPU baseline. Returns threads used. */
+int orc_forward_f32(const OrcModel* m, int64_t n, const float* in, const float* params, const float* max_level,
+                    float max_level_scalar, float* out, int n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

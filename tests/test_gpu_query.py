@@ -1,0 +1,145 @@
+"""Parity of the fused query forward (nlod_inference) against the FP64 oracle.
+
+Tolerances (stated per form, vs the FP64 oracle on identical FP32 weights and inputs):
+  fp32  max |err| <= 2e-5 * (1 + |y|)
+  fp16  mean |err| <= 1e-3, max |err| <= 1e-2 * (1 + |y|)
+  bf16  mean |err| <= 1e-2, max |err| <= 6e-2 * (1 + |y|)
+"""
+import numpy as np
+import pytest
+
+import oracle
+from neural_lod_gb300 import NetworkWithInputEncoding, NlodError, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp32": (2e-5, 2e-5), "fp16": (1e-3, 1e-2), "bf16": (1e-2, 6e-2)}
+
+
+def _check(out, ref, precision):
+    mean_tol, max_tol = TOL[precision]
+    err = np.abs(out.astype(np.float64) - ref)
+    bound = max_tol * (1.0 + np.abs(ref))
+    assert np.all(np.isfinite(out))
+    if precision == "fp32":
+        assert np.all(err <= bound), f"max err {err.max()}"
+    else:
+        assert err.mean() <= mean_tol, f"mean err {err.mean()}"
+        assert np.all(err <= bound), f"max err {err.max()}"
+    return err
+
+
+def _net(cfg, n_in, n_out, precision, seed=3, grid_scale=0.5):
+    enc, net = cfg
+    spec = oracle.model_spec(enc, net, n_in, n_out)
+    params = W.test_params(spec, seed=seed, grid_scale=grid_scale)
+    m = NetworkWithInputEncoding(n_in, n_out, enc, net, precision=precision)
+    m.set_params(params)
+    return m, oracle.Oracle(enc, net, n_in, n_out), params
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16"])
+def test_visibility_query_with_lod_mask(cuda, nlod_lib, precision):
+    import torch
+
+    n = 8192
+    m, orc, params = _net(W.visibility_configs(), 6, 1, precision)
+    x, lod, frac = W.visibility_inputs(n, seed=11)
+    ref = orc.forward(x, params, max_level=frac)
+    xd = torch.from_numpy(x).to(cuda)
+    fd = torch.from_numpy(frac).to(cuda)
+    m.set_max_level_gpu(fd)
+    out = m.inference(xd).cpu().numpy()
+    m.sync_status()
+    _check(out, ref, precision)
+    # masking changes the result (the test is not vacuous)
+    assert np.abs(orc.forward(x, params) - ref).max() > 1e-3
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16"])
+def test_throughput_query(cuda, nlod_lib, precision):
+    import torch
+
+    n = 16384
+    m, orc, params = _net(W.throughput_configs(), 10, 3, precision, grid_scale=0.2)
+    x = W.throughput_inputs(n, seed=5)
+    ref = orc.forward(x, params)
+    out = m.inference(torch.from_numpy(x).to(cuda)).cpu().numpy()
+    m.sync_status()
+    err = _check(out, ref, precision)
+    # per-channel error is reported by the test log
+    print(precision, "per-channel mean abs err", err.mean(axis=0))
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_visibility16_query(cuda, nlod_lib, precision):
+    import torch
+
+    n = 4096
+    m, orc, params = _net(W.visibility_configs(16), 6, 1, precision)
+    x, _, _ = W.visibility_inputs(n, seed=2)
+    ref = orc.forward(x, params)
+    out = m.inference(torch.from_numpy(x).to(cuda)).cpu().numpy()
+    _check(out, ref, precision)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_width128_sh8_config(cuda, nlod_lib, precision):
+    """The shipped arcade throughput configuration shape: 7-level grid (base 8, scale 2),
+    two degree-8 SH encodings (the second one padded first), 128-wide MLP."""
+    import torch
+
+    enc = {"otype": "Composite", "nested": [
+        {"otype": "HashGrid", "n_dims_to_encode": 3, "n_levels": 7, "n_features_per_level": 2, "log2_hashmap_size": 19,
+         "base_resolution": 8, "per_level_scale": 2.0},
+        {"otype": "SphericalHarmonics", "n_dims_to_encode": 3, "degree": 8},
+        {"otype": "SphericalHarmonics", "n_dims_to_encode": 3, "degree": 8}]}
+    net = {"otype": "FullyFusedMLP", "n_neurons": 128, "n_hidden_layers": 4, "activation": "ReLU", "output_activation": "None"}
+    m, orc, params = _net((enc, net), 9, 3, precision, grid_scale=0.3)
+    rng = np.random.default_rng(4)
+    d1 = rng.standard_normal((2048, 3)); d1 /= np.linalg.norm(d1, axis=1, keepdims=True)
+    d2 = rng.standard_normal((2048, 3)); d2 /= np.linalg.norm(d2, axis=1, keepdims=True)
+    x = np.concatenate([rng.random((2048, 3)), (d1 + 1) / 2, (d2 + 1) / 2], axis=1).astype(np.float32)
+    ref = orc.forward(x, params)
+    out = m.inference(torch.from_numpy(x).to(cuda)).cpu().numpy()
+    _check(out, ref, precision)
+
+
+def test_dense_and_nearest_grids(cuda, nlod_lib):
+    import torch
+
+    enc = {"otype": "Composite", "nested": [
+        {"otype": "DenseGrid", "n_dims_to_encode": 3, "n_levels": 4, "base_resolution": 8, "per_level_scale": 1.7,
+         "interpolation": "Nearest"},
+        {"otype": "HashGrid", "n_dims_to_encode": 3, "n_levels": 4, "log2_hashmap_size": 12, "hash": "Prime",
+         "interpolation": "Smoothstep"},
+        {"otype": "Identity", "n_dims_to_encode": 2, "scale": 2.0, "offset": -1.0}]}
+    net = {"otype": "FullyFusedMLP", "n_neurons": 64, "n_hidden_layers": 3, "activation": "ReLU", "output_activation": "None"}
+    for precision in ("fp32", "fp16"):
+        m, orc, params = _net((enc, net), 8, 2, precision, grid_scale=0.5)
+        x = np.random.default_rng(9).random((1024, 8)).astype(np.float32) * 1.2 - 0.1  # some inputs outside [0,1]
+        ref = orc.forward(x, params)
+        out = m.inference(torch.from_numpy(x).to(cuda)).cpu().numpy()
+        _check(out, ref, precision)
+
+
+def test_batch_must_be_multiple_of_128(cuda, nlod_lib):
+    import torch
+
+    m, _, _ = _net(W.visibility_configs(), 6, 1, "fp16")
+    x = torch.zeros((100, 6), device=cuda)
+    with pytest.raises(NlodError) as e:
+        m.inference(x)
+    assert e.value.code == 1
+    # empty batch is a no-op
+    m.inference(torch.zeros((0, 6), device=cuda))
+
+
+def test_deterministic(cuda, nlod_lib):
+    import torch
+
+    m, _, _ = _net(W.throughput_configs(), 10, 3, "fp16", grid_scale=0.2)
+    x = torch.from_numpy(W.throughput_inputs(4096, seed=8)).to(cuda)
+    a = m.inference(x).cpu().numpy()
+    b = m.inference(x).cpu().numpy()
+    assert np.array_equal(a, b)
