@@ -67,7 +67,7 @@ def main():
     print("// Generated by gen_sh.py: real spherical harmonics up to degree 8 (unit directions).")
     print("// Defines SH_BASIS(OUT, x, y, z, degree): OUT(i, value) for i in [0, degree^2).")
     print("#define SH_BASIS(OUT, x, y, z, degree) do { \\")
-    for l in range(9):
+    for l in range(8):
         if l > 0:
             print("  if ((degree) <= %d) break; \\" % l)
         for m in range(-l, l + 1):

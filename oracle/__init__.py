@@ -50,12 +50,33 @@ class OrcAdam(C.Structure):
 _lib = None
 
 
+def declare(L):
+    """Declares argument/return types (pointers must not be narrowed to C int)."""
+    vp, i64, f32, ci = C.c_void_p, C.c_int64, C.c_float, C.c_int
+    L.orc_grid_offsets.restype = C.c_uint32
+    L.orc_grid_offsets.argtypes = [ci, C.c_uint32, C.c_uint32, f32, ci, vp, vp, vp]
+    L.orc_sh.restype = None
+    L.orc_sh.argtypes = [ci, C.c_double, C.c_double, C.c_double, vp]
+    for name in ("orc_encode", "orc_forward"):
+        fn = getattr(L, name)
+        fn.restype = None
+    L.orc_encode.argtypes = [vp, i64, vp, vp, vp, f32, vp]
+    L.orc_forward.argtypes = [vp, i64, vp, vp, vp, f32, vp, vp]
+    L.orc_loss.restype = None
+    L.orc_loss.argtypes = [vp, ci, i64, vp, vp, C.c_double, vp, vp]
+    L.orc_backward.restype = None
+    L.orc_backward.argtypes = [vp, i64, vp, vp, vp, f32, vp, vp]
+    L.orc_adam_step.restype = None
+    L.orc_adam_step.argtypes = [vp, i64, i64, vp, vp, vp, vp, vp, vp, f32, f32, f32]
+    L.orc_forward_f32.restype = ci
+    L.orc_forward_f32.argtypes = [vp, i64, vp, vp, vp, f32, vp, ci]
+    return L
+
+
 def lib():
     global _lib
     if _lib is None:
-        _lib = C.CDLL(str(build_oracle()))
-        _lib.orc_grid_offsets.restype = C.c_uint32
-        _lib.orc_forward_f32.restype = C.c_int
+        _lib = declare(C.CDLL(str(build_oracle())))
     return _lib
 
 
