@@ -1,0 +1,71 @@
+"""Small, self-contained runs of single kernels of the hot path, for ncu captures.
+
+    python -m neural_lod_gb300.profile_run query  [--precision fp16] [--n 2097152] [--iters 3]
+    python -m neural_lod_gb300.profile_run train  [--precision fp16] [--n 262144]  [--iters 3]
+
+`query` runs the throughput-query forward (the bench's headline kernel) `iters` times on the
+bench's inputs; `train` runs visibility training steps.  Each run ends with a status check, so a
+capture only starts after a clean run (the same command without ncu exits 0 first).
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+from pathlib import Path
+
+sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("what", choices=["query", "train", "visq"])
+    ap.add_argument("--precision", default="fp16")
+    ap.add_argument("--n", type=int, default=0)
+    ap.add_argument("--iters", type=int, default=3)
+    a = ap.parse_args()
+
+    import numpy as np
+    import torch
+
+    import neural_lod_gb300 as N
+    from neural_lod_gb300 import workloads as W
+    from neural_lod_gb300.build import build_library
+
+    build_library()
+    dev = torch.device("cuda:0")
+    if a.what == "query":
+        n = a.n or W.WORKLOADS["throughput_query"]["batch"]
+        enc, net = W.throughput_configs()
+        m = N.NetworkWithInputEncoding(10, 3, enc, net, precision=a.precision)
+        x = torch.from_numpy(W.throughput_inputs(n, seed=1)).to(dev)
+        out = torch.empty((n, 3), device=dev)
+        for _ in range(a.iters):
+            m.inference(x, out)
+    elif a.what == "visq":
+        n = a.n or W.WORKLOADS["visibility_query"]["batch"]
+        enc, net = W.visibility_configs()
+        m = N.NetworkWithInputEncoding(6, 1, enc, net, precision=a.precision)
+        xv, _, frac = W.visibility_inputs(n, seed=2)
+        x = torch.from_numpy(xv).to(dev)
+        f = torch.from_numpy(frac).to(dev)
+        m.set_max_level_gpu(f)
+        out = torch.empty((n, 1), device=dev)
+        for _ in range(a.iters):
+            m.inference(x, out)
+    else:
+        n = a.n or W.WORKLOADS["visibility_train"]["batch"]
+        enc, net = W.visibility_configs(16)
+        m = N.NetworkWithInputEncoding(6, 1, enc, net, loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER,
+                                       precision=a.precision)
+        xv, _, _ = W.visibility_inputs(n, seed=3)
+        t = (np.random.default_rng(3).random((n, 1)) < 0.3).astype(np.float32)
+        x, td = torch.from_numpy(xv).to(dev), torch.from_numpy(t).to(dev)
+        for _ in range(a.iters):
+            m.training_step(x, td)
+    m.sync_status()
+    torch.cuda.synchronize()
+    print("ok", a.what, a.precision, n)
+
+
+if __name__ == "__main__":
+    main()
