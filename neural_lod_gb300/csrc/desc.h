@@ -12,7 +12,6 @@ constexpr int kMaxGrids = 2;       // distinct grid encodings (each with its own
 constexpr int kMaxLevels = 32;     // levels per grid (tiny-cuda-nn allows 128; neural_lod uses <= 16)
 constexpr int kMaxLayers = 10;     // weight matrices of the MLP (input + hidden + output)
 constexpr uint32_t kBatchGranularity = 128;
-constexpr int kMaxParts = kMaxGrids * kMaxLevels + kMaxSlots;
 
 enum SlotType : int32_t { SLOT_GRID = 0, SLOT_SH = 1, SLOT_IDENTITY = 2, SLOT_ONEHOT = 3 };
 enum Activation : int32_t { ACT_NONE = 0, ACT_RELU = 1, ACT_SIGMOID = 2, ACT_EXP = 3 };
@@ -28,7 +27,13 @@ struct GridLevel {
     uint32_t size;      // entries in the level ("hashmap_size")
     uint32_t res;       // grid_resolution(scale)
     float scale;        // grid_scale(level, log2(per_level_scale), base_resolution)
+    uint32_t flags;     // kLevelHashed | kLevelPow2 | (dense dims << kLevelDimsShift), precomputed
 };
+
+// Per-level flags: the index rule of grid.h:170-187 resolved once on the host.
+constexpr uint32_t kLevelHashed = 1u;      // the spatial hash replaces the dense index
+constexpr uint32_t kLevelPow2 = 2u;        // size is a power of two (modulo is a mask)
+constexpr uint32_t kLevelDimsShift = 2u;   // dims folded into the dense index (0..3)
 
 struct GridDesc {
     uint32_t n_levels;
@@ -79,10 +84,6 @@ struct ModelDesc {
     uint32_t layer_offset[kMaxLayers];   // first weight of each matrix in the parameter vector
     uint32_t layer_in[kMaxLayers];       // matrix columns
     uint32_t layer_out[kMaxLayers];      // matrix rows
-    // Encoding work list: one part per grid level and one per other slot (see encoding.cuh).
-    uint32_t n_parts;
-    uint8_t part_slot[kMaxParts];
-    uint8_t part_level[kMaxParts];
     Slot slots[kMaxSlots];
     GridDesc grids[kMaxGrids];
 };

@@ -1,6 +1,6 @@
 // Device-side input encodings: multiresolution hash/dense grid, spherical harmonics,
-// identity and one-hot, evaluated per (element, encoding part).  Semantics follow
-// tiny-cuda-nn (paths relative to rptr/ext/tiny-cuda-nn/include/tiny-cuda-nn/):
+// identity and one-hot.  Semantics follow tiny-cuda-nn (paths relative to
+// rptr/ext/tiny-cuda-nn/include/tiny-cuda-nn/):
 //   grid index / hashes       encodings/grid.h:111-187
 //   pos_fract (+0.5 offset)   common_device.h:437-464
 //   forward interpolation     encodings/grid.h:220-392
@@ -9,6 +9,11 @@
 //   spherical harmonics       encodings/spherical_harmonics.h:46-151 (input mapped by 2x-1,
 //                             padding written first as 1.0)
 //   identity                  encodings/identity.h:45-66 (padding written last as 1.0)
+//
+// Work decomposition of a tile: grid slots are evaluated as (row, group of 4 levels) units so one
+// thread has 32 independent table gathers in flight and writes 8 adjacent features at once; the
+// other slots are evaluated as (row, slot) units.  A Store policy (shared-memory layout of the
+// consuming kernel) receives the features.
 #pragma once
 
 #include <cstdint>
@@ -17,7 +22,7 @@
 
 namespace nlod {
 
-// ---- hashing (grid.h:111-187) --------------------------------------------------------------
+// ---- hashing and table index (grid.h:111-187) -----------------------------------------------
 
 __device__ __forceinline__ uint32_t grid_hash3(int32_t kind, uint32_t x, uint32_t y, uint32_t z) {
     // XOR of coordinate * prime; the coherent variant keeps x unscrambled (prime 1).
@@ -26,18 +31,24 @@ __device__ __forceinline__ uint32_t grid_hash3(int32_t kind, uint32_t x, uint32_
     return (x * 2165219737u) ^ (y * 1434869437u) ^ (z * 2097192037u);  // reversed primes
 }
 
-// Table entry of integer grid vertex (x, y, z) within one level: dense row-major index while the
-// running stride fits the level's table, else the spatial hash; always taken modulo the level
-// size.  uint32 wrap-around is part of the definition.
-__device__ __forceinline__ uint32_t grid_entry(const GridDesc& g, const GridLevel& L, uint32_t x, uint32_t y, uint32_t z) {
-    const uint32_t size = L.size;
-    uint32_t stride = 1, index = 0;
-    // dims 0..2, stopping once the stride exceeds the table (avoids overflow at fine levels)
-    if (stride <= size) { index += x * stride; stride *= L.res; }
-    if (stride <= size) { index += y * stride; stride *= L.res; }
-    if (stride <= size) { index += z * stride; stride *= L.res; }
-    if (g.kind == GRID_HASH && size < stride) index = grid_hash3(g.hash, x, y, z);
-    return (size & (size - 1)) == 0 ? (index & (size - 1)) : (index % size);
+// Table entry of integer grid vertex (x, y, z) within one level: the dense row-major index over the
+// dims whose running stride fits the level's table, replaced by the spatial hash on hashed levels,
+// taken modulo the level size.  uint32 wrap-around is part of the definition.
+__device__ __forceinline__ uint32_t level_entry(int32_t hash_kind, const GridLevel& L, uint32_t x, uint32_t y, uint32_t z) {
+    const uint32_t f = L.flags;
+    uint32_t idx;
+    if (f & kLevelHashed) {
+        idx = grid_hash3(hash_kind, x, y, z);
+    } else {
+        const uint32_t dims = f >> kLevelDimsShift;
+        idx = x;
+        if (dims > 1) idx += y * L.res;
+        if (dims > 2) idx += z * (L.res * L.res);
+    }
+    if (f & kLevelPow2) return idx & (L.size - 1u);
+    if (idx < L.size) return idx;
+    const uint32_t t = idx - L.size;   // one wrap covers every vertex of inputs in [0,1]
+    return t < L.size ? t : idx % L.size;
 }
 
 // pos_fract: p = x * scale + 0.5 (a single fused multiply-add), cell = floor(p), frac = p - cell.
@@ -66,45 +77,66 @@ __device__ __forceinline__ bool grid_level_skipped_backward(uint32_t level, floa
     return (float)level > max_level + 1e-3f;
 }
 
-// Trilinear (or nearest) interpolation of the two features of one level.
-// table points at the grid's first float; returns the 2 interpolated features.
-__device__ __forceinline__ float2 grid_level_forward(const GridDesc& g, uint32_t level, const float* __restrict__ table,
-                                                     float px, float py, float pz) {
-    const GridLevel L = g.levels[level];
-    const float2* __restrict__ lv = reinterpret_cast<const float2*>(table) + L.offset;
-    float fx, fy, fz;
-    uint32_t cx, cy, cz;
-    grid_pos_fract(px, L.scale, fx, cx);
-    grid_pos_fract(py, L.scale, fy, cy);
-    grid_pos_fract(pz, L.scale, fz, cz);
-    if (g.interp == INTERP_NEAREST) {
-        return __ldg(lv + grid_entry(g, L, cx, cy, cz));
-    }
-    fx = interp_weight_fun(g.interp, fx);
-    fy = interp_weight_fun(g.interp, fy);
-    fz = interp_weight_fun(g.interp, fz);
-    // Issue all 8 gathers before using any of them.
-    float2 v[8];
+// Features of levels [l0, l0 + nl) (nl <= 4) of one grid for one element: f[2i], f[2i+1] are
+// the two features of level l0 + i.  All gathers of the group are issued before any is used.
+__device__ __forceinline__ void grid_group_forward(const GridDesc& g, uint32_t l0, uint32_t nl, const float* __restrict__ table,
+                                                   float px, float py, float pz, float ml_frac, float (&f)[8]) {
+    const float2* __restrict__ t2 = reinterpret_cast<const float2*>(table);
+    float2 v[4][8];
+    float w3[4][3];
+    bool on[4];
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        v[c] = __ldg(lv + grid_entry(g, L, cx + (c & 1), cy + ((c >> 1) & 1), cz + ((c >> 2) & 1)));
-    }
-    float2 r = make_float2(0.f, 0.f);
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t l = l0 + i;
+        on[i] = (uint32_t)i < nl && !grid_level_masked(l, ml_frac, g.n_levels);
+        if (on[i]) {
+            const GridLevel L = g.levels[l];
+            float fx, fy, fz;
+            uint32_t cx, cy, cz;
+            grid_pos_fract(px, L.scale, fx, cx);
+            grid_pos_fract(py, L.scale, fy, cy);
+            grid_pos_fract(pz, L.scale, fz, cz);
+            w3[i][0] = interp_weight_fun(g.interp, fx);
+            w3[i][1] = interp_weight_fun(g.interp, fy);
+            w3[i][2] = interp_weight_fun(g.interp, fz);
+            const float2* lv = t2 + L.offset;
+            if (g.interp == INTERP_NEAREST) {
+                v[i][0] = __ldg(lv + level_entry(g.hash, L, cx, cy, cz));
+            } else {
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        float w = 1.0f;
-        w *= (c & 1) ? fx : 1.0f - fx;
-        w *= (c & 2) ? fy : 1.0f - fy;
-        w *= (c & 4) ? fz : 1.0f - fz;
-        r.x = fmaf(w, v[c].x, r.x);
-        r.y = fmaf(w, v[c].y, r.y);
+                for (int c = 0; c < 8; ++c)
+                    v[i][c] = __ldg(lv + level_entry(g.hash, L, cx + (c & 1), cy + ((c >> 1) & 1), cz + ((c >> 2) & 1)));
+            }
+        }
     }
-    return r;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float a = 0.f, b = 0.f;
+        if (on[i]) {
+            if (g.interp == INTERP_NEAREST) {
+                a = v[i][0].x;
+                b = v[i][0].y;
+            } else {
+                const float wx[2] = {1.0f - w3[i][0], w3[i][0]};
+                const float wy[2] = {1.0f - w3[i][1], w3[i][1]};
+                const float wz[2] = {1.0f - w3[i][2], w3[i][2]};
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    const float w = wx[c & 1] * wy[(c >> 1) & 1] * wz[(c >> 2) & 1];
+                    a = fmaf(w, v[i][c].x, a);
+                    b = fmaf(w, v[i][c].y, b);
+                }
+            }
+        }
+        f[2 * i] = a;
+        f[2 * i + 1] = b;
+    }
 }
 
 // Scatter dL/d(features) of one level into the FP32 gradient table (grid.h:394-517).
-// Adjacent lanes that hit the same entry are merged before the atomic (warp aggregation),
+// Lanes of a warp that hit the same entry are merged before the atomic (warp aggregation),
 // which matters on the coarse levels where whole warps share a handful of vertices.
+// Must be called by all lanes of the warp (inactive lanes pass active = false).
 __device__ __forceinline__ void grid_level_backward(const GridDesc& g, uint32_t level, float* __restrict__ grad_table,
                                                     float px, float py, float pz, float2 dy, bool active) {
     const GridLevel L = g.levels[level];
@@ -115,30 +147,22 @@ __device__ __forceinline__ void grid_level_backward(const GridDesc& g, uint32_t 
     grid_pos_fract(py, L.scale, fy, cy);
     grid_pos_fract(pz, L.scale, fz, cz);
     const unsigned full = __activemask();
-    if (g.interp == INTERP_NEAREST) {
-        if (active) {
-            uint32_t e = grid_entry(g, L, cx, cy, cz);
-            atomicAdd(reinterpret_cast<float2*>(lv + e), dy);
-        }
-        return;
-    }
+    const int lane = threadIdx.x & 31;
+    const int ncorners = g.interp == INTERP_NEAREST ? 1 : 8;
     fx = interp_weight_fun(g.interp, fx);
     fy = interp_weight_fun(g.interp, fy);
     fz = interp_weight_fun(g.interp, fz);
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        float w = 1.0f;
-        w *= (c & 1) ? fx : 1.0f - fx;
-        w *= (c & 2) ? fy : 1.0f - fy;
-        w *= (c & 4) ? fz : 1.0f - fz;
-        const uint32_t e = active ? grid_entry(g, L, cx + (c & 1), cy + ((c >> 1) & 1), cz + ((c >> 2) & 1)) : 0xFFFFFFFFu;
+    const float wx[2] = {1.0f - fx, fx};
+    const float wy[2] = {1.0f - fy, fy};
+    const float wz[2] = {1.0f - fz, fz};
+    for (int c = 0; c < ncorners; ++c) {
+        const float w = ncorners == 1 ? 1.0f : wx[c & 1] * wy[(c >> 1) & 1] * wz[(c >> 2) & 1];
+        const uint32_t e = active ? level_entry(g.hash, L, cx + (c & 1), cy + ((c >> 1) & 1), cz + ((c >> 2) & 1)) : 0xFFFFFFFFu;
         float2 v = make_float2(active ? w * dy.x : 0.f, active ? w * dy.y : 0.f);
         // Lanes with equal entries form a group; the lowest lane of a group sums the group.
         const unsigned peers = __match_any_sync(full, e);
-        const int lane = threadIdx.x & 31;
         const int leader = __ffs(peers) - 1;
         if (__popc(peers) > 1) {
-            // Sum within the group by walking its members (groups are small except on coarse levels).
             float sx = 0.f, sy = 0.f;
             unsigned m = peers;
             while (m) {
@@ -149,7 +173,7 @@ __device__ __forceinline__ void grid_level_backward(const GridDesc& g, uint32_t 
             }
             v = make_float2(sx, sy);
         }
-        if (active && lane == leader) atomicAdd(reinterpret_cast<float2*>(lv + e), v);
+        if (active && lane == leader) atomicAdd(lv + e, v);
     }
 }
 
@@ -168,30 +192,13 @@ __device__ __forceinline__ void sh_forward(uint32_t degree, float dx01, float dy
 #undef NLOD_SH_OUT
 }
 
-// ---- encoding parts ------------------------------------------------------------------------
-// The encoded row is produced as a list of "parts": one per grid level and one per non-grid
-// slot.  A part writes a fixed set of columns, so parts can be spread over threads.
-
-// Evaluates one part for one element.  `row` is the element's input row, `put(col, value)` stores
-// one encoded feature.  Padding columns of the slot are written by the part of its first level
-// (or by the slot's single part).
+// Evaluates one non-grid slot (or the padding of a grid slot) for one element through put(col, v).
 template <typename Put>
-__device__ __forceinline__ void encode_part(const ModelDesc& d, const float* __restrict__ params, uint32_t slot_idx,
-                                            uint32_t level, const float* __restrict__ row, float max_level_frac, Put&& put) {
-    const Slot& s = d.slots[slot_idx];
+__device__ __forceinline__ void encode_slot_scalar(const Slot& s, const ModelDesc& d, const float* __restrict__ row, Put&& put) {
     switch (s.type) {
         case SLOT_GRID: {
-            const GridDesc& g = d.grids[s.grid];
-            const uint32_t nf = g.n_levels * 2u;
-            if (level == 0) {
-                for (uint32_t p = 0; p < s.n_pad; ++p) put(s.out_begin + nf + p, 0.0f);
-            }
-            float2 r = make_float2(0.f, 0.f);
-            if (!grid_level_masked(level, max_level_frac, g.n_levels)) {
-                r = grid_level_forward(g, level, params + g.param_offset, row[s.in_begin], row[s.in_begin + 1], row[s.in_begin + 2]);
-            }
-            put(s.out_begin + 2 * level, r.x);
-            put(s.out_begin + 2 * level + 1, r.y);
+            const uint32_t nf = d.grids[s.grid].n_levels * 2u;
+            for (uint32_t p = 0; p < s.n_pad; ++p) put(s.out_begin + nf + p, 0.0f);
             break;
         }
         case SLOT_SH: {
@@ -215,6 +222,38 @@ __device__ __forceinline__ void encode_part(const ModelDesc& d, const float* __r
             break;
         }
         default: break;
+    }
+}
+
+// Encodes `rows` staged input rows (in_s, row stride in_ld) into the consumer's tile.
+// Store must provide: run8(r, col, const float (&f)[8], n) storing f[0..n) at columns col..col+n
+// (col even, n even) and one(r, col, v).
+template <typename Store>
+__device__ __forceinline__ void encode_tile(const ModelDesc& d, const float* __restrict__ params, const float* in_s, uint32_t in_ld,
+                                            const float* __restrict__ ml_gpu, float ml_scalar, uint32_t row0, uint32_t rows,
+                                            uint32_t tid, uint32_t nthreads, Store& st) {
+    for (uint32_t si = 0; si < d.n_slots; ++si) {
+        const Slot& s = d.slots[si];
+        if (s.type != SLOT_GRID) continue;
+        const GridDesc& g = d.grids[s.grid];
+        const uint32_t ngroups = (g.n_levels + 3u) / 4u;
+        const float* table = params + g.param_offset;
+        for (uint32_t u = tid; u < rows * ngroups; u += nthreads) {
+            const uint32_t r = u % rows, grp = u / rows;
+            const float* row = in_s + r * in_ld + s.in_begin;
+            const float ml = ml_gpu ? __ldg(ml_gpu + row0 + r) : ml_scalar;
+            const uint32_t l0 = grp * 4u;
+            const uint32_t nl = min(4u, g.n_levels - l0);
+            float f[8];
+            grid_group_forward(g, l0, nl, table, row[0], row[1], row[2], ml, f);
+            st.run8(r, s.out_begin + 2u * l0, f, 2u * nl);
+        }
+    }
+    for (uint32_t u = tid; u < rows * d.n_slots; u += nthreads) {
+        const uint32_t r = u % rows, si = u / rows;
+        const Slot& s = d.slots[si];
+        if (s.type == SLOT_GRID && s.n_pad == 0) continue;
+        encode_slot_scalar(s, d, in_s + r * in_ld, [&](uint32_t col, float v) { st.one(r, col, v); });
     }
 }
 

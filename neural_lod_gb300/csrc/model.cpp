@@ -176,6 +176,17 @@ void build_grid(const Json& j, uint32_t n_dims, EncNode& n) {
         g.levels[i].size = in_level;
         g.levels[i].res = res;
         g.levels[i].scale = scale;
+        // grid_index's loop (grid.h:175-186): dims are folded while the running stride fits.
+        uint32_t dims = 0;
+        uint32_t stride32 = 1;
+        for (uint32_t dim = 0; dim < 3 && stride32 <= in_level; ++dim) {
+            ++dims;
+            stride32 *= res;   // uint32 arithmetic, as on the device
+        }
+        uint32_t flags = dims << kLevelDimsShift;
+        if (g.kind == GRID_HASH && in_level < stride32) flags |= kLevelHashed;
+        if ((in_level & (in_level - 1)) == 0) flags |= kLevelPow2;
+        g.levels[i].flags = flags;
         if ((uint64_t)offset + in_level > 0x7FFFFFFFull) throw std::runtime_error("GridEncoding: too many parameters");
         offset += in_level;
     }
@@ -359,15 +370,6 @@ void build_model_desc(const Json& encoding, const Json& network, uint32_t n_inpu
 
     Flattener f{d};
     f.flatten(root, 0);
-    for (uint32_t i = 0; i < d.n_slots; ++i) {
-        const uint32_t parts = d.slots[i].type == SLOT_GRID ? d.grids[d.slots[i].grid].n_levels : 1u;
-        for (uint32_t p = 0; p < parts; ++p) {
-            if (d.n_parts >= (uint32_t)kMaxParts) throw std::runtime_error("encoding: too many parts");
-            d.part_slot[d.n_parts] = (uint8_t)i;
-            d.part_level[d.n_parts] = (uint8_t)p;
-            ++d.n_parts;
-        }
-    }
     d.enc_width = root.padded_output_width();
     if (d.enc_width != f.out_cursor) throw std::runtime_error("internal: encoding width mismatch");
     if (d.enc_width % 16 != 0 || d.enc_width == 0 || d.enc_width > 256)

@@ -108,6 +108,24 @@ struct LayerBlock {
     }
 };
 
+// Encoded features as FP32 into a row-major shared tile.
+struct SimtStore {
+    float* act;
+    uint32_t lda;
+    __device__ __forceinline__ void run8(uint32_t r, uint32_t col, const float (&f)[8], uint32_t n) {
+        float* dst = act + r * lda + col;
+        if (n == 8 && (col & 3u) == 0) {
+            *reinterpret_cast<float4*>(dst) = make_float4(f[0], f[1], f[2], f[3]);
+            *reinterpret_cast<float4*>(dst + 4) = make_float4(f[4], f[5], f[6], f[7]);
+        } else {
+#pragma unroll
+            for (uint32_t i = 0; i < 8; ++i)
+                if (i < n) dst[i] = f[i];
+        }
+    }
+    __device__ __forceinline__ void one(uint32_t r, uint32_t col, float v) { act[r * lda + col] = v; }
+};
+
 // Loads W [out][in] (row-major, global) transposed into WT[in][out] in shared memory.
 __device__ __forceinline__ void load_weights_transposed(const float* __restrict__ W, int n_out, int n_in, float* WT) {
     for (int idx = threadIdx.x; idx < n_out * n_in; idx += kThreads) {
@@ -171,13 +189,10 @@ __global__ void __launch_bounds__(kThreads) k_forward_simt(const __grid_constant
             in_s[r * L.lda_in + c] = in_tile[idx];
         }
         __syncthreads();
-        // 2. encoding: one (element, part) pair per thread iteration
-        for (uint32_t u = threadIdx.x; u < kTile * d.n_parts; u += kThreads) {
-            const uint32_t r = u % kTile, part = u / kTile;
-            const float ml = a.max_level_gpu ? a.max_level_gpu[row0 + r] : a.max_level;
-            float* dst = act_a + r * L.lda_a;
-            encode_part(d, a.params, d.part_slot[part], d.part_level[part], in_s + r * L.lda_in, ml,
-                        [&](uint32_t col, float v) { dst[col] = v; });
+        // 2. encoding into act_a
+        {
+            SimtStore st{act_a, (uint32_t)L.lda_a};
+            encode_tile(d, a.params, in_s, (uint32_t)L.lda_in, a.max_level_gpu, a.max_level, row0, kTile, threadIdx.x, kThreads, st);
         }
         __syncthreads();
         if (a.enc) {

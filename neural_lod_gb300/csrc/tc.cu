@@ -1,16 +1,19 @@
 // Tensor-core form of the fused neural-LoD query: encoding + fully fused MLP on tcgen05.
 //
-// One CTA (8 warps) owns a 128-element tile at a time (persistent grid-stride loop):
+// A CTA holds every weight matrix of the network in shared memory (loaded once, FP16/BF16,
+// K-major core-matrix layout) and runs two independent 4-warp tile pipelines ("groups").  Each
+// group owns a 128-element tile at a time (persistent grid-stride loop), its own A-operand
+// buffer, staged inputs, mbarrier and half of the CTA's TMEM:
 //   1. the tile's input rows are staged in shared memory (one coalesced copy);
-//   2. all 256 threads evaluate (element, encoding part) pairs and write the encoded tile as the
-//      MMA A operand (FP16/BF16, K-major no-swizzle core-matrix layout);
+//   2. the group's 128 threads evaluate the encoding ((row, 4-level group) units for grids,
+//      (row, slot) units otherwise) straight into the A operand;
 //   3. per layer, one thread issues K/16 tcgen05.mma (M=128, N=width or 16, FP32 accumulate in
-//      TMEM) and commits them to an mbarrier; after the wait every warp reads its 32-lane TMEM
-//      quarter (tcgen05.ld), applies the activation, converts and writes the next A operand back
-//      into the same shared buffer (the MMA has finished reading it);
+//      TMEM) and commits them to the group's mbarrier; after the wait each of the 4 warps reads
+//      its 32-lane TMEM quarter (tcgen05.ld), applies the activation, converts and writes the
+//      next A operand back into the same buffer (the MMAs have finished reading it);
 //   4. the 16-wide output layer's epilogue applies the output activation and writes FP32 rows.
-// All weights of the network stay resident in shared memory for the CTA's lifetime; several CTAs
-// per SM overlap one CTA's gather-bound encoding with another's MMA chain.
+// While one group runs its serial MMA/epilogue chain the other group's gather-bound encoding
+// keeps the SM busy; two CTAs per SM give four such pipelines.
 //
 // The math is tiny-cuda-nn's FullyFusedMLP forward (rptr/ext/tiny-cuda-nn/src/fully_fused_mlp.cu:499-633)
 // with FP32 instead of FP16 accumulation, fed by the composite encoding of encoding.cuh.
@@ -30,18 +33,22 @@ namespace nlod {
 namespace {
 
 constexpr int kTcTile = 128;
-constexpr int kTcThreads = 256;
+constexpr int kGroups = 2;
+constexpr int kGroupThreads = 128;
+constexpr int kTcThreads = kGroups * kGroupThreads;
 constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 
+// Shared-memory plan.  Layer l's B operand starts at byte 2 * layer_offset[l]: the network's
+// matrices are contiguous and each is a multiple of 16 x 16 elements (512 bytes).
 struct TcLayout {
-    uint32_t w_off[kMaxLayers];   // byte offset of each layer's B operand
     uint32_t w_bytes;
-    uint32_t a_off;               // A operand tile
+    uint32_t a_off[kGroups];      // A operand tile of each group
     uint32_t a_bytes;
-    uint32_t in_off;              // staged input rows (FP32)
+    uint32_t in_off[kGroups];     // staged input rows (FP32) of each group
     uint32_t in_ld;
-    uint32_t bar_off;
+    uint32_t bar_off;             // kGroups mbarriers, then the TMEM base address
     uint32_t total;
+    uint32_t tmem_group_cols;     // TMEM columns per group (accumulator W + output 16)
     uint32_t tmem_cols;
 };
 
@@ -49,26 +56,68 @@ __host__ __device__ inline uint32_t align_up(uint32_t v, uint32_t a) { return (v
 
 __host__ __device__ inline TcLayout tc_layout(const ModelDesc& d) {
     TcLayout L{};
-    uint32_t off = 0;
-    for (uint32_t l = 0; l < d.n_layers; ++l) {
-        L.w_off[l] = off;
-        off += d.layer_in[l] * d.layer_out[l] * 2u;
-        off = align_up(off, 128);
-    }
+    uint32_t off = align_up(d.n_params_network * 2u, 128);
     L.w_bytes = off;
-    L.a_off = off;
     const uint32_t ka = d.enc_width > d.width ? d.enc_width : d.width;
     L.a_bytes = kTcTile * ka * 2u;
-    off = align_up(off + L.a_bytes, 128);
-    L.in_off = off;
     L.in_ld = d.n_input + 1;
-    off = align_up(off + kTcTile * L.in_ld * 4u, 16);
+    for (int g = 0; g < kGroups; ++g) {
+        L.a_off[g] = off;
+        off = align_up(off + L.a_bytes, 128);
+        L.in_off[g] = off;
+        off = align_up(off + kTcTile * L.in_ld * 4u, 128);
+    }
     L.bar_off = off;
-    off += 16;   // mbarrier (8) + TMEM base address (4) + timeout flag (4)
+    off += 8 * kGroups + 8;
     L.total = align_up(off, 128);
-    L.tmem_cols = d.width + 16 <= 128 ? 128u : 256u;
+    L.tmem_group_cols = d.width + 16 <= 128 ? 128u : 256u;
+    L.tmem_cols = kGroups * L.tmem_group_cols;
     return L;
 }
+
+// Named barrier over the 128 threads of one group (id 1 + group; id 0 is __syncthreads).
+__device__ __forceinline__ void group_sync(uint32_t id) {
+    asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory");
+}
+
+// Group barrier that also ORs a predicate over the group's threads.
+__device__ __forceinline__ bool group_sync_or(uint32_t id, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id)
+        : "memory");
+    return r != 0;
+}
+
+// Encoded features as FP16/BF16 into the K-major core-matrix A operand.
+template <typename T>
+struct TcStore {
+    uint8_t* tile;
+    uint32_t sbo;
+    __device__ __forceinline__ void run8(uint32_t r, uint32_t col, const float (&f)[8], uint32_t n) {
+        using Op = tc::OpType<T>;
+        if (n == 8 && (col & 7u) == 0) {
+            uint4 pk;
+            pk.x = Op::pack2(f[0], f[1]);
+            pk.y = Op::pack2(f[2], f[3]);
+            pk.z = Op::pack2(f[4], f[5]);
+            pk.w = Op::pack2(f[6], f[7]);
+            *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(r, col, sbo)) = pk;
+        } else {
+#pragma unroll
+            for (uint32_t i = 0; i < 4; ++i)
+                if (2 * i < n) *reinterpret_cast<uint32_t*>(tile + tc::kmajor_offset(r, col + 2 * i, sbo)) = Op::pack2(f[2 * i], f[2 * i + 1]);
+        }
+    }
+    __device__ __forceinline__ void one(uint32_t r, uint32_t col, float v) {
+        *reinterpret_cast<uint16_t*>(tile + tc::kmajor_offset(r, col, sbo)) = tc::OpType<T>::pack1(v);
+    }
+};
 
 __device__ __forceinline__ float act_fwd(int32_t act, float v) {
     switch (act) {
@@ -80,22 +129,24 @@ __device__ __forceinline__ float act_fwd(int32_t act, float v) {
 }
 
 template <int W, typename T>
-__global__ void __launch_bounds__(kTcThreads) k_forward_tc(const __grid_constant__ ModelDesc d, const __grid_constant__ ForwardArgs a,
-                                                           uint32_t* __restrict__ status) {
+__global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_constant__ ModelDesc d, const __grid_constant__ ForwardArgs a,
+                                                              uint32_t* __restrict__ status) {
     using Op = tc::OpType<T>;
     extern __shared__ __align__(1024) uint8_t smem[];
     const TcLayout L = tc_layout(d);
-    uint8_t* a_tile = smem + L.a_off;
-    float* in_s = reinterpret_cast<float*>(smem + L.in_off);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L.bar_off);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 8);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bar_off);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 8 * kGroups);
 
     const uint32_t tid = threadIdx.x;
     const uint32_t warp = tid >> 5, lane = tid & 31;
+    const uint32_t grp = warp >> 2;              // tile pipeline of this thread
+    const uint32_t gtid = tid & (kGroupThreads - 1);
+    const uint32_t quarter = warp & 3u;          // TMEM lane quarter this warp may access
+    const uint32_t bar_id = 1u + grp;
 
-    // ---- set-up: barrier, TMEM, resident weights ----
+    // ---- set-up: barriers, TMEM, resident weights ----
     if (tid == 0) {
-        tc::mbar_init(bar, 1);
+        for (int g = 0; g < kGroups; ++g) tc::mbar_init(&bars[g], 1);
         tc::fence_barrier_init();
     }
     if (warp == 0) {
@@ -112,7 +163,7 @@ __global__ void __launch_bounds__(kTcThreads) k_forward_tc(const __grid_constant
             const uint4* src = reinterpret_cast<const uint4*>(wsrc + d.layer_offset[l]);
             for (uint32_t c = tid; c < chunks; c += kTcThreads) {
                 const uint32_t n = c / (K / 8u), k0 = (c - n * (K / 8u)) * 8u;
-                *reinterpret_cast<uint4*>(smem + L.w_off[l] + tc::kmajor_offset(n, k0, sbo)) = src[c];
+                *reinterpret_cast<uint4*>(smem + 2u * d.layer_offset[l] + tc::kmajor_offset(n, k0, sbo)) = src[c];
             }
         }
     }
@@ -120,39 +171,35 @@ __global__ void __launch_bounds__(kTcThreads) k_forward_tc(const __grid_constant
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem_base = *tmem_slot;
+    const uint32_t tmem_base = *tmem_slot + grp * L.tmem_group_cols;
+    uint8_t* a_tile = smem + L.a_off[grp];
+    float* in_s = reinterpret_cast<float*>(smem + L.in_off[grp]);
+    uint64_t* bar = &bars[grp];
     const uint32_t a_addr = tc::smem_addr(a_tile);
 
     uint32_t phase = 0;
     bool aborted = false;
     const uint32_t n_tiles = a.n / kTcTile;
-    const uint32_t quarter = warp & 3u, half = warp >> 2;
     const uint32_t row = quarter * 32u + lane;   // TMEM lane == tile row owned in the epilogue
+    const uint32_t taddr_row = tmem_base + ((quarter * 32u) << 16);
 
-    for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    for (uint32_t tile = blockIdx.x * kGroups + grp; tile < n_tiles; tile += gridDim.x * kGroups) {
         const uint32_t row0 = tile * kTcTile;
         // 1. stage inputs
         const float* in_tile = a.in + (size_t)row0 * d.n_input;
-        for (uint32_t idx = tid; idx < kTcTile * d.n_input; idx += kTcThreads) {
+        for (uint32_t idx = gtid; idx < kTcTile * d.n_input; idx += kGroupThreads) {
             const uint32_t r = idx / d.n_input, c = idx - r * d.n_input;
-            in_s[r * L.in_ld + c] = in_tile[idx];
+            in_s[r * L.in_ld + c] = __ldg(in_tile + idx);
         }
-        __syncthreads();
+        group_sync(bar_id);
         // 2. encoding into the A operand (K = enc_width)
         {
-            const uint32_t sbo = d.enc_width * 16u;
-            for (uint32_t u = tid; u < kTcTile * d.n_parts; u += kTcThreads) {
-                const uint32_t r = u % kTcTile, part = u / kTcTile;
-                const float ml = a.max_level_gpu ? a.max_level_gpu[row0 + r] : a.max_level;
-                encode_part(d, a.params, d.part_slot[part], d.part_level[part], in_s + r * L.in_ld, ml,
-                            [&](uint32_t col, float v) {
-                                *reinterpret_cast<uint16_t*>(a_tile + tc::kmajor_offset(r, col, sbo)) = Op::pack1(v);
-                            });
-            }
+            TcStore<T> st{a_tile, d.enc_width * 16u};
+            encode_tile(d, a.params, in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile, gtid, kGroupThreads, st);
         }
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
-        __syncthreads();
+        group_sync(bar_id);
 
         // 3. layer chain
         for (uint32_t l = 0; l < d.n_layers; ++l) {
@@ -161,10 +208,10 @@ __global__ void __launch_bounds__(kTcThreads) k_forward_tc(const __grid_constant
             const uint32_t N = d.layer_out[l];
             const uint32_t sbo = K * 16u;
             const uint32_t d_col = last ? (uint32_t)W : 0u;
-            if (tid == 0) {
+            if (gtid == 0) {
                 tc::fence_after_sync();
                 const uint32_t idesc = tc::make_idesc_f16(Op::kFmt, kTcTile, N);
-                const uint32_t b_addr = tc::smem_addr(smem + L.w_off[l]);
+                const uint32_t b_addr = tc::smem_addr(smem + 2u * d.layer_offset[l]);
                 for (uint32_t k = 0; k < K; k += 16) {
                     const uint64_t adesc = tc::make_smem_desc(a_addr + (k / 8u) * 128u, 128u, sbo);
                     const uint64_t bdesc = tc::make_smem_desc(b_addr + (k / 8u) * 128u, 128u, sbo);
@@ -174,17 +221,15 @@ __global__ void __launch_bounds__(kTcThreads) k_forward_tc(const __grid_constant
             }
             const bool ok = tc::mbar_wait_bounded(bar, phase, kWaitCycles);
             phase ^= 1u;
-            // Uniform decision: every thread has finished its own bounded wait here.
-            if (__syncthreads_or(!ok)) { aborted = true; break; }
+            // Uniform decision within the group: every thread has finished its bounded wait.
+            if (group_sync_or(bar_id, !ok)) { aborted = true; break; }
             tc::fence_after_sync();
 
-            const uint32_t taddr_row = tmem_base + ((quarter * 32u) << 16);
             if (!last) {
-                // hidden epilogue: warp (quarter, half) converts columns [half*W/2, (half+1)*W/2)
+                // hidden epilogue: each warp converts all W columns of its 32 rows
                 const uint32_t out_sbo = (uint32_t)W * 16u;
 #pragma unroll
-                for (uint32_t c0 = 0; c0 < (uint32_t)W / 2u; c0 += 32) {
-                    const uint32_t col = half * ((uint32_t)W / 2u) + c0;
+                for (uint32_t col = 0; col < (uint32_t)W; col += 32) {
                     uint32_t r[32];
                     tc::tmem_ld32(taddr_row + col, r);
                     tc::tmem_wait_ld();
@@ -199,7 +244,7 @@ __global__ void __launch_bounds__(kTcThreads) k_forward_tc(const __grid_constant
                     }
                 }
                 tc::fence_proxy_async_smem();
-            } else if (half == 0) {
+            } else {
                 uint32_t r[16];
                 tc::tmem_ld16(taddr_row + d_col, r);
                 tc::tmem_wait_ld();
@@ -217,22 +262,22 @@ __global__ void __launch_bounds__(kTcThreads) k_forward_tc(const __grid_constant
                 }
             }
             tc::fence_before_sync();
-            __syncthreads();
+            group_sync(bar_id);
         }
         if (aborted) break;
     }
 
     // ---- teardown ----
     if (aborted) {
-        // Give the outstanding MMAs one more bounded chance to finish before TMEM is released.
+        // Give the group's outstanding MMAs one more bounded chance to finish before TMEM is released.
         (void)tc::mbar_wait_bounded(bar, phase ^ 1u, kWaitCycles);
-        if (tid == 0) atomicOr(status, 1u);
+        if (gtid == 0) atomicOr(status, 1u);
     }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(tmem_base, L.tmem_cols);
+        tc::tmem_dealloc(*tmem_slot, L.tmem_cols);
     }
 }
 
@@ -247,7 +292,7 @@ int sm_count() {
     return g_sms;
 }
 
-// Dynamic shared memory request: what the tile needs, raised so that TMEM (512 columns per SM)
+// Dynamic shared memory request: what the tiles need, raised so that TMEM (512 columns per SM)
 // can never be over-subscribed by co-resident CTAs.
 size_t tc_smem_bytes(const ModelDesc& d, int* per_sm_out) {
     const TcLayout L = tc_layout(d);
@@ -279,7 +324,8 @@ cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind
     const size_t bytes = tc_smem_bytes(d, &per_sm);
     const uint32_t n_tiles = a.n / kTcTile;
     uint32_t blocks = (uint32_t)(per_sm * sm_count());
-    if (blocks > n_tiles) blocks = n_tiles;
+    const uint32_t need = (n_tiles + kGroups - 1) / kGroups;
+    if (blocks > need) blocks = need;
     if (blocks == 0) return cudaSuccess;
     cudaError_t e = cudaSuccess;
 #define NLOD_TC_CASE(WD, TY)                                                                          \
