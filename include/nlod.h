@@ -184,6 +184,17 @@ NLOD_API int  nlod_serialize(nlod_module* m, int half_precision, char** json_out
 NLOD_API int  nlod_deserialize(nlod_module* m, const char* json);
 NLOD_API void nlod_free_string(char* s);
 
+/*
+ * Kernel organisation of the tensor-core query (tile pipelines per CTA x grid levels per gather
+ * unit).  No tiny-cuda-nn counterpart (its launch shapes are fixed).  nlod_autotune times every
+ * variant that fits the network on the given batch (synchronous, runs the query 4 times per
+ * variant) and keeps the fastest; nlod_set_kernel_variant forces one.  The FP32 form has one.
+ */
+NLOD_API int nlod_kernel_variants(const nlod_module* m);
+NLOD_API int nlod_get_kernel_variant(const nlod_module* m);
+NLOD_API int nlod_set_kernel_variant(nlod_module* m, int variant);
+NLOD_API int nlod_autotune(nlod_module* m, void* stream, uint32_t n, const float* in, float* out);
+
 /* Device status word of the last launch sequence (NLOD_OK or NLOD_ERR_TIMEOUT); synchronises. */
 NLOD_API int nlod_sync_status(nlod_module* m, void* stream);
 

@@ -146,6 +146,28 @@ class NetworkWithInputEncoding:
     def backward(self, ctx, x, dL_dout, stream=None) -> None:
         check(self._lib.nlod_backward(self._m, _stream_ptr(stream), ctx.handle, _ptr(x), _ptr(dL_dout)))
 
+    # ---- kernel variants / autotuning ------------------------------------------------------
+    @property
+    def n_kernel_variants(self) -> int:
+        return int(self._lib.nlod_kernel_variants(self._m))
+
+    @property
+    def kernel_variant(self) -> int:
+        return int(self._lib.nlod_get_kernel_variant(self._m))
+
+    @kernel_variant.setter
+    def kernel_variant(self, v: int) -> None:
+        check(self._lib.nlod_set_kernel_variant(self._m, int(v)))
+
+    def autotune(self, x, out=None, stream=None) -> int:
+        """Times every kernel variant on batch x and keeps the fastest; returns its index."""
+        import torch
+
+        if out is None:
+            out = torch.empty((x.shape[0], self.n_output_dims), device=x.device, dtype=torch.float32)
+        check(self._lib.nlod_autotune(self._m, _stream_ptr(stream), x.shape[0], _ptr(x), _ptr(out)))
+        return self.kernel_variant
+
     def sync_status(self, stream=None) -> None:
         check(self._lib.nlod_sync_status(self._m, _stream_ptr(stream)))
 

@@ -56,6 +56,10 @@ SIGNATURES = [
     ("nlod_serialize", C.c_int, [_vp, C.c_int, C.POINTER(C.c_void_p)]),
     ("nlod_deserialize", C.c_int, [_vp, C.c_char_p]),
     ("nlod_free_string", None, [C.c_void_p]),
+    ("nlod_kernel_variants", C.c_int, [_vp]),
+    ("nlod_get_kernel_variant", C.c_int, [_vp]),
+    ("nlod_set_kernel_variant", C.c_int, [_vp, C.c_int]),
+    ("nlod_autotune", C.c_int, [_vp, _vp, _u32, _fp, _fp]),
     ("nlod_sync_status", C.c_int, [_vp, _vp]),
 ]
 

@@ -118,6 +118,7 @@ struct nlod_module {
     float grad_scale = 1.0f;
 
     Workspace ws;
+    int tc_variant = -1;            // tensor-core kernel organisation (autotuned or default)
 
     const float* inference_params() const { return ema ? ema : params; }
     int op_kind() const { return precision == NLOD_PRECISION_FP16 ? 1 : 2; }
@@ -305,8 +306,11 @@ int nlod_module_create(const char* encoding_json, const char* network_json, cons
             m->base_lr = m->opt.adam.learning_rate;
         }
         m->precision = precision;
-        if (precision != NLOD_PRECISION_FP32 && !tc_supported(m->d))
-            throw Error(NLOD_ERR_UNSUPPORTED, "tensor-core form needs n_neurons 64 or 128 and an encoded width <= 256");
+        if (precision != NLOD_PRECISION_FP32) {
+            if (!tc_supported(m->d))
+                throw Error(NLOD_ERR_UNSUPPORTED, "tensor-core form needs n_neurons 64 or 128 and an encoded width <= 256");
+            m->tc_variant = tc_default_variant(m->d);
+        }
         const size_t np = m->d.n_params;
         m->n_params = (uint32_t)np;
         try {
@@ -467,7 +471,7 @@ int nlod_inference(nlod_module* m, void* stream, uint32_t n, const float* in, fl
         ForwardArgs a = base_forward_args(m, n, in, true);
         a.out = out;
         if (m->precision == NLOD_PRECISION_FP32) cuda_check(launch_forward_simt(m->d, a, 0, s), "inference");
-        else cuda_check(launch_forward_tc(m->d, a, m->op_kind(), m->status, s), "inference");
+        else cuda_check(launch_forward_tc(m->d, a, m->op_kind(), m->tc_variant, m->status, s), "inference");
     });
 }
 
@@ -728,6 +732,56 @@ int nlod_deserialize(nlod_module* m, const char* json) {
 }
 
 void nlod_free_string(char* s) { std::free(s); }
+
+int nlod_kernel_variants(const nlod_module* m) {
+    if (!m || m->precision == NLOD_PRECISION_FP32) return 1;
+    return tc_num_variants();
+}
+
+int nlod_set_kernel_variant(nlod_module* m, int variant) {
+    return guarded([&] {
+        if (!m) throw Error(NLOD_ERR_INVALID, "module is NULL");
+        if (m->precision == NLOD_PRECISION_FP32) {
+            if (variant != 0) throw Error(NLOD_ERR_INVALID, "the FP32 form has a single kernel variant");
+            return;
+        }
+        if (!tc_variant_ok(m->d, variant)) throw Error(NLOD_ERR_UNSUPPORTED, "kernel variant does not fit this network");
+        m->tc_variant = variant;
+    });
+}
+
+int nlod_get_kernel_variant(const nlod_module* m) { return m ? (m->precision == NLOD_PRECISION_FP32 ? 0 : m->tc_variant) : -1; }
+
+int nlod_autotune(nlod_module* m, void* stream, uint32_t n, const float* in, float* out) {
+    return guarded([&] {
+        if (!m) throw Error(NLOD_ERR_INVALID, "module is NULL");
+        check_batch(n);
+        if (n == 0 || m->precision == NLOD_PRECISION_FP32) return;
+        if (!in || !out) throw Error(NLOD_ERR_INVALID, "input and output must not be NULL");
+        cudaStream_t s = (cudaStream_t)stream;
+        cudaEvent_t e0, e1;
+        cuda_check(cudaEventCreate(&e0), "event");
+        cuda_check(cudaEventCreate(&e1), "event");
+        float best = 3.0e38f;
+        int best_v = m->tc_variant;
+        ForwardArgs a = base_forward_args(m, n, in, true);
+        a.out = out;
+        for (int v = 0; v < tc_num_variants(); ++v) {
+            if (!tc_variant_ok(m->d, v)) continue;
+            cuda_check(launch_forward_tc(m->d, a, m->op_kind(), v, m->status, s), "autotune");
+            cuda_check(cudaEventRecord(e0, s), "event");
+            for (int it = 0; it < 3; ++it) cuda_check(launch_forward_tc(m->d, a, m->op_kind(), v, m->status, s), "autotune");
+            cuda_check(cudaEventRecord(e1, s), "event");
+            cuda_check(cudaEventSynchronize(e1), "event");
+            float ms = 0.f;
+            cuda_check(cudaEventElapsedTime(&ms, e0, e1), "event");
+            if (ms < best) { best = ms; best_v = v; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        m->tc_variant = best_v;
+    });
+}
 
 int nlod_sync_status(nlod_module* m, void* stream) {
     if (!m) {

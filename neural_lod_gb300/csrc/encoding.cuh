@@ -77,16 +77,67 @@ __device__ __forceinline__ bool grid_level_skipped_backward(uint32_t level, floa
     return (float)level > max_level + 1e-3f;
 }
 
-// Features of levels [l0, l0 + nl) (nl <= 4) of one grid for one element: f[2i], f[2i+1] are
-// the two features of level l0 + i.  All gathers of the group are issued before any is used.
-__device__ __forceinline__ void grid_group_forward(const GridDesc& g, uint32_t l0, uint32_t nl, const float* __restrict__ table,
-                                                   float px, float py, float pz, float ml_frac, float (&f)[8]) {
-    const float2* __restrict__ t2 = reinterpret_cast<const float2*>(table);
-    float2 v[4][8];
-    float w3[4][3];
-    bool on[4];
+__device__ __forceinline__ void hash_primes(int32_t kind, uint32_t& p0, uint32_t& p1, uint32_t& p2) {
+    if (kind == HASH_COHERENT_PRIME) { p0 = 1u; p1 = 2654435761u; p2 = 805459861u; }
+    else if (kind == HASH_PRIME) { p0 = 1958374283u; p1 = 2654435761u; p2 = 805459861u; }
+    else { p0 = 2165219737u; p1 = 1434869437u; p2 = 2097192037u; }
+}
+
+// Reduces a dense index modulo a non power-of-two level size (one subtraction covers inputs in
+// [0,1]; anything else takes the division).
+__device__ __forceinline__ uint32_t dense_mod(uint32_t idx, uint32_t size) {
+    if (idx < size) return idx;
+    const uint32_t t = idx - size;
+    return t < size ? t : idx % size;
+}
+
+// Table entries of the 8 corners of the cell (cx, cy, cz) at one level: corner c takes
+// (cx + (c&1), cy + (c>>1 & 1), cz + (c>>2 & 1)).  The per-axis terms of the index (dense
+// strides or hash products) are formed once and combined per corner, which is exactly
+// level_entry() for each corner.
+__device__ __forceinline__ void level_corner_entries(const GridLevel& L, uint32_t p0, uint32_t p1, uint32_t p2, uint32_t cx,
+                                                     uint32_t cy, uint32_t cz, uint32_t (&e)[8]) {
+    const uint32_t f = L.flags;
+    if (f & kLevelHashed) {
+        // hashed levels always have a power-of-two size
+        const uint32_t m = L.size - 1u;
+        const uint32_t x0 = cx * p0, x1 = (cx + 1u) * p0;
+        const uint32_t y0 = cy * p1, y1 = (cy + 1u) * p1;
+        const uint32_t z0 = cz * p2, z1 = (cz + 1u) * p2;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+        for (int c = 0; c < 8; ++c) e[c] = ((c & 1) ? x1 : x0) ^ ((c & 2) ? y1 : y0) ^ ((c & 4) ? z1 : z0);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) e[c] &= m;
+    } else {
+        const uint32_t dims = f >> kLevelDimsShift;
+        const uint32_t sy = dims > 1 ? L.res : 0u, sz = dims > 2 ? L.res * L.res : 0u;
+        const uint32_t y0 = cy * sy, y1 = (cy + 1u) * sy;
+        const uint32_t z0 = cz * sz, z1 = (cz + 1u) * sz;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) e[c] = ((c & 1) ? cx + 1u : cx) + ((c & 2) ? y1 : y0) + ((c & 4) ? z1 : z0);
+        if (f & kLevelPow2) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) e[c] &= L.size - 1u;
+        } else {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) e[c] = dense_mod(e[c], L.size);
+        }
+    }
+}
+
+// Features of levels [l0, l0 + nl) (nl <= NL) of one grid for one element: f[2i], f[2i+1] are
+// the two features of level l0 + i.  All gathers of the group are issued before any is used.
+template <int NL>
+__device__ __forceinline__ void grid_group_forward(const GridDesc& g, uint32_t l0, uint32_t nl, const float* __restrict__ table,
+                                                   float px, float py, float pz, float ml_frac, float (&f)[2 * NL]) {
+    const float2* __restrict__ t2 = reinterpret_cast<const float2*>(table);
+    uint32_t p0, p1, p2;
+    hash_primes(g.hash, p0, p1, p2);
+    float2 v[NL][8];
+    float w3[NL][3];
+    bool on[NL];
+#pragma unroll
+    for (int i = 0; i < NL; ++i) {
         const uint32_t l = l0 + i;
         on[i] = (uint32_t)i < nl && !grid_level_masked(l, ml_frac, g.n_levels);
         if (on[i]) {
@@ -103,26 +154,27 @@ __device__ __forceinline__ void grid_group_forward(const GridDesc& g, uint32_t l
             if (g.interp == INTERP_NEAREST) {
                 v[i][0] = __ldg(lv + level_entry(g.hash, L, cx, cy, cz));
             } else {
+                uint32_t e[8];
+                level_corner_entries(L, p0, p1, p2, cx, cy, cz, e);
 #pragma unroll
-                for (int c = 0; c < 8; ++c)
-                    v[i][c] = __ldg(lv + level_entry(g.hash, L, cx + (c & 1), cy + ((c >> 1) & 1), cz + ((c >> 2) & 1)));
+                for (int c = 0; c < 8; ++c) v[i][c] = __ldg(lv + e[c]);
             }
         }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < NL; ++i) {
         float a = 0.f, b = 0.f;
         if (on[i]) {
             if (g.interp == INTERP_NEAREST) {
                 a = v[i][0].x;
                 b = v[i][0].y;
             } else {
-                const float wx[2] = {1.0f - w3[i][0], w3[i][0]};
-                const float wy[2] = {1.0f - w3[i][1], w3[i][1]};
-                const float wz[2] = {1.0f - w3[i][2], w3[i][2]};
+                const float wx0 = 1.0f - w3[i][0], wx1 = w3[i][0];
+                const float wy0 = 1.0f - w3[i][1], wy1 = w3[i][1];
+                const float wz0 = 1.0f - w3[i][2], wz1 = w3[i][2];
 #pragma unroll
                 for (int c = 0; c < 8; ++c) {
-                    const float w = wx[c & 1] * wy[(c >> 1) & 1] * wz[(c >> 2) & 1];
+                    const float w = ((c & 1) ? wx1 : wx0) * ((c & 2) ? wy1 : wy0) * ((c & 4) ? wz1 : wz0);
                     a = fmaf(w, v[i][c].x, a);
                     b = fmaf(w, v[i][c].y, b);
                 }
@@ -225,10 +277,11 @@ __device__ __forceinline__ void encode_slot_scalar(const Slot& s, const ModelDes
     }
 }
 
-// Encodes `rows` staged input rows (in_s, row stride in_ld) into the consumer's tile.
-// Store must provide: run8(r, col, const float (&f)[8], n) storing f[0..n) at columns col..col+n
-// (col even, n even) and one(r, col, v).
-template <typename Store>
+// Encodes `rows` staged input rows (in_s, row stride in_ld) into the consumer's tile; each grid
+// unit covers NL levels (NL = 2 or 4).
+// Store must provide: run(r, col, const float (&f)[2*NL], n) storing f[0..n) at columns
+// col..col+n (col even, n even) and one(r, col, v).
+template <int NL, typename Store>
 __device__ __forceinline__ void encode_tile(const ModelDesc& d, const float* __restrict__ params, const float* in_s, uint32_t in_ld,
                                             const float* __restrict__ ml_gpu, float ml_scalar, uint32_t row0, uint32_t rows,
                                             uint32_t tid, uint32_t nthreads, Store& st) {
@@ -236,17 +289,17 @@ __device__ __forceinline__ void encode_tile(const ModelDesc& d, const float* __r
         const Slot& s = d.slots[si];
         if (s.type != SLOT_GRID) continue;
         const GridDesc& g = d.grids[s.grid];
-        const uint32_t ngroups = (g.n_levels + 3u) / 4u;
+        const uint32_t ngroups = (g.n_levels + NL - 1u) / NL;
         const float* table = params + g.param_offset;
         for (uint32_t u = tid; u < rows * ngroups; u += nthreads) {
             const uint32_t r = u % rows, grp = u / rows;
             const float* row = in_s + r * in_ld + s.in_begin;
             const float ml = ml_gpu ? __ldg(ml_gpu + row0 + r) : ml_scalar;
-            const uint32_t l0 = grp * 4u;
-            const uint32_t nl = min(4u, g.n_levels - l0);
-            float f[8];
-            grid_group_forward(g, l0, nl, table, row[0], row[1], row[2], ml, f);
-            st.run8(r, s.out_begin + 2u * l0, f, 2u * nl);
+            const uint32_t l0 = grp * NL;
+            const uint32_t nl = min((uint32_t)NL, g.n_levels - l0);
+            float f[2 * NL];
+            grid_group_forward<NL>(g, l0, nl, table, row[0], row[1], row[2], ml, f);
+            st.run(r, s.out_begin + 2u * l0, f, 2u * nl);
         }
     }
     for (uint32_t u = tid; u < rows * d.n_slots; u += nthreads) {

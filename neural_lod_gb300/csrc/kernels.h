@@ -99,8 +99,12 @@ struct AdamStepArgs {
 };
 cudaError_t launch_adam_step(const AdamStepArgs& a, cudaStream_t s);
 
-// Tensor-core (tcgen05) forms.  kind 1 = FP16, 2 = BF16.
+// Tensor-core (tcgen05) forms.  kind 1 = FP16, 2 = BF16.  `variant` selects the CTA
+// organisation (tile pipelines per CTA, grid levels per gather unit); see tc.cu.
 bool tc_supported(const ModelDesc& d);
-cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, uint32_t* status, cudaStream_t s);
+int tc_num_variants();
+bool tc_variant_ok(const ModelDesc& d, int variant);
+int tc_default_variant(const ModelDesc& d);
+cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, int variant, uint32_t* status, cudaStream_t s);
 
 }  // namespace nlod

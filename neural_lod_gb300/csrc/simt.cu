@@ -112,14 +112,15 @@ struct LayerBlock {
 struct SimtStore {
     float* act;
     uint32_t lda;
-    __device__ __forceinline__ void run8(uint32_t r, uint32_t col, const float (&f)[8], uint32_t n) {
+    template <int M>
+    __device__ __forceinline__ void run(uint32_t r, uint32_t col, const float (&f)[M], uint32_t n) {
         float* dst = act + r * lda + col;
-        if (n == 8 && (col & 3u) == 0) {
-            *reinterpret_cast<float4*>(dst) = make_float4(f[0], f[1], f[2], f[3]);
-            *reinterpret_cast<float4*>(dst + 4) = make_float4(f[4], f[5], f[6], f[7]);
+        if (n == (uint32_t)M && (col & 3u) == 0) {
+#pragma unroll
+            for (int i = 0; i < M; i += 4) *reinterpret_cast<float4*>(dst + i) = make_float4(f[i], f[i + 1], f[i + 2], f[i + 3]);
         } else {
 #pragma unroll
-            for (uint32_t i = 0; i < 8; ++i)
+            for (uint32_t i = 0; i < (uint32_t)M; ++i)
                 if (i < n) dst[i] = f[i];
         }
     }
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(kThreads) k_forward_simt(const __grid_constant
         // 2. encoding into act_a
         {
             SimtStore st{act_a, (uint32_t)L.lda_a};
-            encode_tile(d, a.params, in_s, (uint32_t)L.lda_in, a.max_level_gpu, a.max_level, row0, kTile, threadIdx.x, kThreads, st);
+            encode_tile<2>(d, a.params, in_s, (uint32_t)L.lda_in, a.max_level_gpu, a.max_level, row0, kTile, threadIdx.x, kThreads, st);
         }
         __syncthreads();
         if (a.enc) {

@@ -1,19 +1,20 @@
 // Tensor-core form of the fused neural-LoD query: encoding + fully fused MLP on tcgen05.
 //
 // A CTA holds every weight matrix of the network in shared memory (loaded once, FP16/BF16,
-// K-major core-matrix layout) and runs two independent 4-warp tile pipelines ("groups").  Each
+// K-major core-matrix layout) and runs G independent 4-warp tile pipelines ("groups").  Each
 // group owns a 128-element tile at a time (persistent grid-stride loop), its own A-operand
-// buffer, staged inputs, mbarrier and half of the CTA's TMEM:
+// buffer, staged inputs, mbarrier and W columns of the CTA's TMEM:
 //   1. the tile's input rows are staged in shared memory (one coalesced copy);
-//   2. the group's 128 threads evaluate the encoding ((row, 4-level group) units for grids,
+//   2. the group's 128 threads evaluate the encoding ((row, NL-level group) units for grids,
 //      (row, slot) units otherwise) straight into the A operand;
 //   3. per layer, one thread issues K/16 tcgen05.mma (M=128, N=width or 16, FP32 accumulate in
 //      TMEM) and commits them to the group's mbarrier; after the wait each of the 4 warps reads
 //      its 32-lane TMEM quarter (tcgen05.ld), applies the activation, converts and writes the
 //      next A operand back into the same buffer (the MMAs have finished reading it);
-//   4. the 16-wide output layer's epilogue applies the output activation and writes FP32 rows.
-// While one group runs its serial MMA/epilogue chain the other group's gather-bound encoding
-// keeps the SM busy; two CTAs per SM give four such pipelines.
+//   4. the 16-wide output layer (accumulated into the same TMEM columns, which the previous
+//      epilogue has drained) applies the output activation and writes FP32 rows.
+// While one group runs its serial MMA/epilogue chain the other groups' gather-bound encodings keep
+// the SM busy.  (G, NL) variants are instantiated and chosen by a measured autotune.
 //
 // The math is tiny-cuda-nn's FullyFusedMLP forward (rptr/ext/tiny-cuda-nn/src/fully_fused_mlp.cu:499-633)
 // with FP32 instead of FP16 accumulation, fed by the composite encoding of encoding.cuh.
@@ -33,45 +34,40 @@ namespace nlod {
 namespace {
 
 constexpr int kTcTile = 128;
-constexpr int kGroups = 2;
 constexpr int kGroupThreads = 128;
-constexpr int kTcThreads = kGroups * kGroupThreads;
 constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 
 // Shared-memory plan.  Layer l's B operand starts at byte 2 * layer_offset[l]: the network's
 // matrices are contiguous and each is a multiple of 16 x 16 elements (512 bytes).
 struct TcLayout {
-    uint32_t w_bytes;
-    uint32_t a_off[kGroups];      // A operand tile of each group
-    uint32_t a_bytes;
-    uint32_t in_off[kGroups];     // staged input rows (FP32) of each group
+    uint32_t w_bytes;             // resident weights; group g's region starts at w_bytes + g * group_stride
+    uint32_t a_bytes;             // A operand tile (first in a group's region)
+    uint32_t in_rel;              // staged input rows (FP32), relative to the region
     uint32_t in_ld;
-    uint32_t bar_off;             // kGroups mbarriers, then the TMEM base address
+    uint32_t group_stride;
+    uint32_t bar_off;             // G mbarriers, then the TMEM base address
     uint32_t total;
-    uint32_t tmem_group_cols;     // TMEM columns per group (accumulator W + output 16)
-    uint32_t tmem_cols;
+    uint32_t tmem_cols;           // G * width rounded up to a power of two
 };
 
 __host__ __device__ inline uint32_t align_up(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
 
-__host__ __device__ inline TcLayout tc_layout(const ModelDesc& d) {
+__host__ __device__ inline TcLayout tc_layout(const ModelDesc& d, int G) {
     TcLayout L{};
     uint32_t off = align_up(d.n_params_network * 2u, 128);
     L.w_bytes = off;
     const uint32_t ka = d.enc_width > d.width ? d.enc_width : d.width;
     L.a_bytes = kTcTile * ka * 2u;
     L.in_ld = d.n_input + 1;
-    for (int g = 0; g < kGroups; ++g) {
-        L.a_off[g] = off;
-        off = align_up(off + L.a_bytes, 128);
-        L.in_off[g] = off;
-        off = align_up(off + kTcTile * L.in_ld * 4u, 128);
-    }
+    L.in_rel = align_up(L.a_bytes, 128);
+    L.group_stride = L.in_rel + align_up(kTcTile * L.in_ld * 4u, 128);
+    off += (uint32_t)G * L.group_stride;
     L.bar_off = off;
-    off += 8 * kGroups + 8;
+    off += 8 * G + 8;
     L.total = align_up(off, 128);
-    L.tmem_group_cols = d.width + 16 <= 128 ? 128u : 256u;
-    L.tmem_cols = kGroups * L.tmem_group_cols;
+    uint32_t cols = 32;
+    while (cols < (uint32_t)G * d.width) cols <<= 1;   // TMEM allocations are powers of two
+    L.tmem_cols = cols;
     return L;
 }
 
@@ -99,18 +95,27 @@ template <typename T>
 struct TcStore {
     uint8_t* tile;
     uint32_t sbo;
-    __device__ __forceinline__ void run8(uint32_t r, uint32_t col, const float (&f)[8], uint32_t n) {
+    template <int M>
+    __device__ __forceinline__ void run(uint32_t r, uint32_t col, const float (&f)[M], uint32_t n) {
         using Op = tc::OpType<T>;
-        if (n == 8 && (col & 7u) == 0) {
-            uint4 pk;
+        if (M % 8 == 0 && n == (uint32_t)M && (col & 7u) == 0) {
+#pragma unroll
+            for (int i = 0; i < M; i += 8) {
+                uint4 pk;
+                pk.x = Op::pack2(f[i + 0], f[i + 1]);
+                pk.y = Op::pack2(f[i + 2], f[i + 3]);
+                pk.z = Op::pack2(f[i + 4], f[i + 5]);
+                pk.w = Op::pack2(f[i + 6], f[i + 7]);
+                *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(r, col + i, sbo)) = pk;
+            }
+        } else if (M == 4 && n == 4 && (col & 3u) == 0) {
+            uint2 pk;
             pk.x = Op::pack2(f[0], f[1]);
-            pk.y = Op::pack2(f[2], f[3]);
-            pk.z = Op::pack2(f[4], f[5]);
-            pk.w = Op::pack2(f[6], f[7]);
-            *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(r, col, sbo)) = pk;
+            pk.y = Op::pack2(f[2 % M], f[3 % M]);
+            *reinterpret_cast<uint2*>(tile + tc::kmajor_offset(r, col, sbo)) = pk;
         } else {
 #pragma unroll
-            for (uint32_t i = 0; i < 4; ++i)
+            for (uint32_t i = 0; i < (uint32_t)M / 2; ++i)
                 if (2 * i < n) *reinterpret_cast<uint32_t*>(tile + tc::kmajor_offset(r, col + 2 * i, sbo)) = Op::pack2(f[2 * i], f[2 * i + 1]);
         }
     }
@@ -128,14 +133,16 @@ __device__ __forceinline__ float act_fwd(int32_t act, float v) {
     }
 }
 
-template <int W, typename T>
-__global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_constant__ ModelDesc d, const __grid_constant__ ForwardArgs a,
-                                                              uint32_t* __restrict__ status) {
+template <int W, typename T, int G, int NL>
+__global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward_tc(const __grid_constant__ ModelDesc d,
+                                                                                    const __grid_constant__ ForwardArgs a,
+                                                                                    uint32_t* __restrict__ status) {
     using Op = tc::OpType<T>;
+    constexpr int kThreads = G * kGroupThreads;
     extern __shared__ __align__(1024) uint8_t smem[];
-    const TcLayout L = tc_layout(d);
+    const TcLayout L = tc_layout(d, G);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bar_off);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 8 * kGroups);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 8 * G);
 
     const uint32_t tid = threadIdx.x;
     const uint32_t warp = tid >> 5, lane = tid & 31;
@@ -146,7 +153,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
 
     // ---- set-up: barriers, TMEM, resident weights ----
     if (tid == 0) {
-        for (int g = 0; g < kGroups; ++g) tc::mbar_init(&bars[g], 1);
+        for (int g = 0; g < G; ++g) tc::mbar_init(&bars[g], 1);
         tc::fence_barrier_init();
     }
     if (warp == 0) {
@@ -161,7 +168,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
             const uint32_t sbo = K * 16u;
             const uint32_t chunks = N * (K / 8u);
             const uint4* src = reinterpret_cast<const uint4*>(wsrc + d.layer_offset[l]);
-            for (uint32_t c = tid; c < chunks; c += kTcThreads) {
+            for (uint32_t c = tid; c < chunks; c += kThreads) {
                 const uint32_t n = c / (K / 8u), k0 = (c - n * (K / 8u)) * 8u;
                 *reinterpret_cast<uint4*>(smem + 2u * d.layer_offset[l] + tc::kmajor_offset(n, k0, sbo)) = src[c];
             }
@@ -171,9 +178,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem_base = *tmem_slot + grp * L.tmem_group_cols;
-    uint8_t* a_tile = smem + L.a_off[grp];
-    float* in_s = reinterpret_cast<float*>(smem + L.in_off[grp]);
+    const uint32_t tmem_base = *tmem_slot + grp * (uint32_t)W;
+    uint8_t* a_tile = smem + L.w_bytes + grp * L.group_stride;
+    float* in_s = reinterpret_cast<float*>(a_tile + L.in_rel);
     uint64_t* bar = &bars[grp];
     const uint32_t a_addr = tc::smem_addr(a_tile);
 
@@ -183,7 +190,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
     const uint32_t row = quarter * 32u + lane;   // TMEM lane == tile row owned in the epilogue
     const uint32_t taddr_row = tmem_base + ((quarter * 32u) << 16);
 
-    for (uint32_t tile = blockIdx.x * kGroups + grp; tile < n_tiles; tile += gridDim.x * kGroups) {
+    for (uint32_t tile = blockIdx.x * G + grp; tile < n_tiles; tile += gridDim.x * G) {
         const uint32_t row0 = tile * kTcTile;
         // 1. stage inputs
         const float* in_tile = a.in + (size_t)row0 * d.n_input;
@@ -195,7 +202,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
         // 2. encoding into the A operand (K = enc_width)
         {
             TcStore<T> st{a_tile, d.enc_width * 16u};
-            encode_tile(d, a.params, in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile, gtid, kGroupThreads, st);
+            encode_tile<NL>(d, a.params, in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile, gtid, kGroupThreads, st);
         }
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
@@ -207,7 +214,6 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
             const uint32_t K = d.layer_in[l];
             const uint32_t N = d.layer_out[l];
             const uint32_t sbo = K * 16u;
-            const uint32_t d_col = last ? (uint32_t)W : 0u;
             if (gtid == 0) {
                 tc::fence_after_sync();
                 const uint32_t idesc = tc::make_idesc_f16(Op::kFmt, kTcTile, N);
@@ -215,7 +221,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
                 for (uint32_t k = 0; k < K; k += 16) {
                     const uint64_t adesc = tc::make_smem_desc(a_addr + (k / 8u) * 128u, 128u, sbo);
                     const uint64_t bdesc = tc::make_smem_desc(b_addr + (k / 8u) * 128u, 128u, sbo);
-                    tc::mma_f16_ss(tmem_base + d_col, adesc, bdesc, idesc, k > 0 ? 1u : 0u);
+                    tc::mma_f16_ss(tmem_base, adesc, bdesc, idesc, k > 0 ? 1u : 0u);
                 }
                 tc::mma_commit(bar);
             }
@@ -246,7 +252,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
                 tc::fence_proxy_async_smem();
             } else {
                 uint32_t r[16];
-                tc::tmem_ld16(taddr_row + d_col, r);
+                tc::tmem_ld16(taddr_row, r);
                 tc::tmem_wait_ld();
                 const size_t grow = (size_t)row0 + row;
                 if (a.out) {
@@ -294,8 +300,8 @@ int sm_count() {
 
 // Dynamic shared memory request: what the tiles need, raised so that TMEM (512 columns per SM)
 // can never be over-subscribed by co-resident CTAs.
-size_t tc_smem_bytes(const ModelDesc& d, int* per_sm_out) {
-    const TcLayout L = tc_layout(d);
+size_t tc_smem_bytes(const ModelDesc& d, int G, int* per_sm_out) {
+    const TcLayout L = tc_layout(d, G);
     const uint32_t cap = 512u / L.tmem_cols;               // CTAs whose TMEM fits on one SM
     const size_t sm_bytes = 233472;                        // 228 KB per SM
     size_t bytes = L.total;
@@ -309,38 +315,70 @@ size_t tc_smem_bytes(const ModelDesc& d, int* per_sm_out) {
     return bytes;
 }
 
+struct Variant {
+    int G, NL;
+};
+constexpr Variant kVariants[] = {{2, 2}, {2, 4}, {4, 2}, {4, 4}, {6, 2}};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+
+template <int W, typename T, int G, int NL>
+cudaError_t launch_variant(const ModelDesc& d, const ForwardArgs& a, uint32_t* status, cudaStream_t s) {
+    int per_sm = 1;
+    const size_t bytes = tc_smem_bytes(d, G, &per_sm);
+    if (bytes > 227u * 1024u || per_sm < 1) return cudaErrorInvalidConfiguration;
+    const uint32_t n_tiles = a.n / kTcTile;
+    uint32_t blocks = (uint32_t)(per_sm * sm_count());
+    const uint32_t need = (n_tiles + G - 1) / G;
+    if (blocks > need) blocks = need;
+    if (blocks == 0) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_forward_tc<W, T, G, NL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    k_forward_tc<W, T, G, NL><<<blocks, G * kGroupThreads, bytes, s>>>(d, a, status);
+    return cudaGetLastError();
+}
+
+template <int W, typename T>
+cudaError_t launch_typed(const ModelDesc& d, const ForwardArgs& a, int variant, uint32_t* status, cudaStream_t s) {
+    switch (variant) {
+        case 0: return launch_variant<W, T, 2, 2>(d, a, status, s);
+        case 1: return launch_variant<W, T, 2, 4>(d, a, status, s);
+        case 2: return launch_variant<W, T, 4, 2>(d, a, status, s);
+        case 3: return launch_variant<W, T, 4, 4>(d, a, status, s);
+        case 4: return launch_variant<W, T, 6, 2>(d, a, status, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 }  // namespace
+
+int tc_num_variants() { return kNumVariants; }
+
+bool tc_variant_ok(const ModelDesc& d, int variant) {
+    if (variant < 0 || variant >= kNumVariants) return false;
+    int per_sm = 0;
+    const size_t bytes = tc_smem_bytes(d, kVariants[variant].G, &per_sm);
+    return bytes <= 227u * 1024u && per_sm >= 1 && (uint32_t)kVariants[variant].G * d.width <= 512u;
+}
+
+int tc_default_variant(const ModelDesc& d) {
+    for (int v = 0; v < kNumVariants; ++v)
+        if (tc_variant_ok(d, v)) return v;
+    return -1;
+}
 
 bool tc_supported(const ModelDesc& d) {
     if (d.width != 64 && d.width != 128) return false;
     if (d.enc_width % 16 != 0 || d.enc_width > 256) return false;
-    int per_sm = 0;
-    const size_t bytes = tc_smem_bytes(d, &per_sm);
-    return bytes <= 227u * 1024u && per_sm >= 1;
+    return tc_default_variant(d) >= 0;
 }
 
-cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, uint32_t* status, cudaStream_t s) {
-    int per_sm = 1;
-    const size_t bytes = tc_smem_bytes(d, &per_sm);
-    const uint32_t n_tiles = a.n / kTcTile;
-    uint32_t blocks = (uint32_t)(per_sm * sm_count());
-    const uint32_t need = (n_tiles + kGroups - 1) / kGroups;
-    if (blocks > need) blocks = need;
-    if (blocks == 0) return cudaSuccess;
-    cudaError_t e = cudaSuccess;
-#define NLOD_TC_CASE(WD, TY)                                                                          \
-    do {                                                                                              \
-        e = cudaFuncSetAttribute(k_forward_tc<WD, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes); \
-        if (e != cudaSuccess) return e;                                                               \
-        k_forward_tc<WD, TY><<<blocks, kTcThreads, bytes, s>>>(d, a, status);                         \
-    } while (0)
-    if (d.width == 64 && kind == 1) NLOD_TC_CASE(64, __half);
-    else if (d.width == 64 && kind == 2) NLOD_TC_CASE(64, __nv_bfloat16);
-    else if (d.width == 128 && kind == 1) NLOD_TC_CASE(128, __half);
-    else if (d.width == 128 && kind == 2) NLOD_TC_CASE(128, __nv_bfloat16);
-    else return cudaErrorInvalidValue;
-#undef NLOD_TC_CASE
-    return cudaGetLastError();
+cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, int variant, uint32_t* status, cudaStream_t s) {
+    if (!tc_variant_ok(d, variant)) return cudaErrorInvalidValue;
+    if (d.width == 64 && kind == 1) return launch_typed<64, __half>(d, a, variant, status, s);
+    if (d.width == 64 && kind == 2) return launch_typed<64, __nv_bfloat16>(d, a, variant, status, s);
+    if (d.width == 128 && kind == 1) return launch_typed<128, __half>(d, a, variant, status, s);
+    if (d.width == 128 && kind == 2) return launch_typed<128, __nv_bfloat16>(d, a, variant, status, s);
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace nlod

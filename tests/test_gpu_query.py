@@ -123,6 +123,34 @@ def test_dense_and_nearest_grids(cuda, nlod_lib):
         _check(out, ref, precision)
 
 
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+def test_every_kernel_variant_and_autotune(cuda, nlod_lib, precision):
+    """Each tensor-core kernel organisation the autotuner may pick computes the same result."""
+    import torch
+
+    m, orc, params = _net(W.throughput_configs(), 10, 3, precision, grid_scale=0.2)
+    x = W.throughput_inputs(8192 + 128 * 5, seed=6)   # tile count not a multiple of any group count
+    ref = orc.forward(x, params)
+    xd = torch.from_numpy(x).to(cuda)
+    outs = []
+    assert m.n_kernel_variants >= 4
+    for v in range(m.n_kernel_variants):
+        try:
+            m.kernel_variant = v
+        except NlodError as e:
+            assert e.code == 4  # variant does not fit this network
+            continue
+        out = m.inference(xd).cpu().numpy()
+        m.sync_status()
+        _check(out, ref, precision)
+        outs.append(out)
+    assert len(outs) >= 4
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])  # same arithmetic in every organisation
+    best = m.autotune(xd)
+    assert 0 <= best < m.n_kernel_variants
+
+
 def test_batch_must_be_multiple_of_128(cuda, nlod_lib):
     import torch
 
