@@ -306,7 +306,25 @@ __device__ __forceinline__ void encode_tile(const ModelDesc& d, const float* __r
         const uint32_t r = u % rows, si = u / rows;
         const Slot& s = d.slots[si];
         if (s.type == SLOT_GRID && s.n_pad == 0) continue;
-        encode_slot_scalar(s, d, in_s + r * in_ld, [&](uint32_t col, float v) { st.one(r, col, v); });
+        const float* row = in_s + r * in_ld;
+        if (s.type == SLOT_SH && s.degree == 4 && s.n_pad == 0 && (s.out_begin & 1u) == 0) {
+            // 16 values in registers, stored as whole runs
+            float v[16];
+            sh_forward(4u, row[s.in_begin], row[s.in_begin + 1], row[s.in_begin + 2], [&](uint32_t i, float x) { v[i] = x; });
+            st.run(r, s.out_begin, v, 16u);
+            continue;
+        }
+        if (s.type == SLOT_ONEHOT && s.out_width <= 16u && (s.out_width & 1u) == 0 && (s.out_begin & 1u) == 0) {
+            // one-hot bins followed by zero padding, stored as one run
+            float v[16];
+            int bin = (int)floorf(row[s.in_begin] * (float)s.n_bins);
+            bin = bin < 0 ? 0 : (bin >= (int)s.n_bins ? (int)s.n_bins - 1 : bin);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = j == bin ? 1.0f : 0.0f;
+            st.run(r, s.out_begin, v, s.out_width);
+            continue;
+        }
+        encode_slot_scalar(s, d, row, [&](uint32_t col, float v) { st.one(r, col, v); });
     }
 }
 

@@ -318,7 +318,7 @@ size_t tc_smem_bytes(const ModelDesc& d, int G, int* per_sm_out) {
 struct Variant {
     int G, NL;
 };
-constexpr Variant kVariants[] = {{2, 2}, {2, 4}, {4, 2}, {4, 4}, {6, 2}};
+constexpr Variant kVariants[] = {{2, 2}, {2, 4}, {4, 2}, {4, 4}, {6, 2}, {5, 2}, {6, 1}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 template <int W, typename T, int G, int NL>
@@ -345,6 +345,8 @@ cudaError_t launch_typed(const ModelDesc& d, const ForwardArgs& a, int variant, 
         case 2: return launch_variant<W, T, 4, 2>(d, a, status, s);
         case 3: return launch_variant<W, T, 4, 4>(d, a, status, s);
         case 4: return launch_variant<W, T, 6, 2>(d, a, status, s);
+        case 5: return launch_variant<W, T, 5, 2>(d, a, status, s);
+        case 6: return launch_variant<W, T, 6, 1>(d, a, status, s);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -22,6 +22,7 @@ def main():
     ap.add_argument("--precision", default="fp16")
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--iters", type=int, default=3)
+    ap.add_argument("--variant", type=int, default=-1, help="tensor-core kernel variant (-1: autotune)")
     a = ap.parse_args()
 
     import numpy as np
@@ -39,6 +40,11 @@ def main():
         m = N.NetworkWithInputEncoding(10, 3, enc, net, precision=a.precision)
         x = torch.from_numpy(W.throughput_inputs(n, seed=1)).to(dev)
         out = torch.empty((n, 3), device=dev)
+        if a.variant >= 0:
+            m.kernel_variant = a.variant
+        elif a.precision != "fp32":
+            m.autotune(x, out)
+        print("variant", m.kernel_variant)
         for _ in range(a.iters):
             m.inference(x, out)
     elif a.what == "visq":
