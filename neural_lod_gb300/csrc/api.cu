@@ -14,7 +14,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/nlod.h"
+#include "nlod.h"
 #include "desc.h"
 #include "json.h"
 #include "kernels.h"
@@ -404,7 +404,7 @@ int nlod_layout_json(const char* encoding_json, const char* network_json, uint32
             Json off = Json::array(), res = Json::array(), sc = Json::array();
             for (uint32_t l = 0; l < gd.n_levels; ++l) {
                 off.push(Json::number(gd.levels[l].offset));
-                res.push(Json::number(gd.levels[l].res));
+                res.push(Json::number(gd.levels[l].res_flags & kLevelResMask));
                 sc.push(Json::number(gd.levels[l].scale));
             }
             off.push(Json::number(gd.levels[gd.n_levels - 1].offset + gd.levels[gd.n_levels - 1].size));

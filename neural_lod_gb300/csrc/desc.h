@@ -22,18 +22,20 @@ enum LossKind : int32_t { LOSS_NONE = 0, LOSS_BCE = 1, LOSS_RELATIVE_L2 = 2, LOS
 
 // One level of a grid encoding: tiny-cuda-nn's offset table entry plus the derived
 // per-level scale and resolution (rptr/ext/tiny-cuda-nn/include/tiny-cuda-nn/encodings/grid.h:195-204, 982-1015).
-struct GridLevel {
+// 16 bytes, so a kernel reads one level with a single 128-bit shared-memory load.
+struct alignas(16) GridLevel {
     uint32_t offset;    // first table entry of the level (entries, not floats)
     uint32_t size;      // entries in the level ("hashmap_size")
-    uint32_t res;       // grid_resolution(scale)
+    uint32_t res_flags; // grid_resolution(scale) in bits 0..27, per-level flags in bits 28..31
     float scale;        // grid_scale(level, log2(per_level_scale), base_resolution)
-    uint32_t flags;     // kLevelHashed | kLevelPow2 | (dense dims << kLevelDimsShift), precomputed
 };
 
-// Per-level flags: the index rule of grid.h:170-187 resolved once on the host.
-constexpr uint32_t kLevelHashed = 1u;      // the spatial hash replaces the dense index
-constexpr uint32_t kLevelPow2 = 2u;        // size is a power of two (modulo is a mask)
-constexpr uint32_t kLevelDimsShift = 2u;   // dims folded into the dense index (0..3)
+// Per-level flags (bits 28..31 of res_flags): the index rule of grid.h:170-187 resolved once on
+// the host.
+constexpr uint32_t kLevelResMask = 0x0FFFFFFFu;
+constexpr uint32_t kLevelHashed = 1u << 28;     // the spatial hash replaces the dense index
+constexpr uint32_t kLevelPow2 = 1u << 29;       // size is a power of two (modulo is a mask)
+constexpr uint32_t kLevelDimsShift = 30u;       // dims folded into the dense index (0..3)
 
 struct GridDesc {
     uint32_t n_levels;

@@ -35,15 +35,16 @@ __device__ __forceinline__ uint32_t grid_hash3(int32_t kind, uint32_t x, uint32_
 // dims whose running stride fits the level's table, replaced by the spatial hash on hashed levels,
 // taken modulo the level size.  uint32 wrap-around is part of the definition.
 __device__ __forceinline__ uint32_t level_entry(int32_t hash_kind, const GridLevel& L, uint32_t x, uint32_t y, uint32_t z) {
-    const uint32_t f = L.flags;
+    const uint32_t f = L.res_flags;
+    const uint32_t res = f & kLevelResMask;
     uint32_t idx;
     if (f & kLevelHashed) {
         idx = grid_hash3(hash_kind, x, y, z);
     } else {
         const uint32_t dims = f >> kLevelDimsShift;
         idx = x;
-        if (dims > 1) idx += y * L.res;
-        if (dims > 2) idx += z * (L.res * L.res);
+        if (dims > 1) idx += y * res;
+        if (dims > 2) idx += z * (res * res);
     }
     if (f & kLevelPow2) return idx & (L.size - 1u);
     if (idx < L.size) return idx;
@@ -97,7 +98,7 @@ __device__ __forceinline__ uint32_t dense_mod(uint32_t idx, uint32_t size) {
 // level_entry() for each corner.
 __device__ __forceinline__ void level_corner_entries(const GridLevel& L, uint32_t p0, uint32_t p1, uint32_t p2, uint32_t cx,
                                                      uint32_t cy, uint32_t cz, uint32_t (&e)[8]) {
-    const uint32_t f = L.flags;
+    const uint32_t f = L.res_flags;
     if (f & kLevelHashed) {
         // hashed levels always have a power-of-two size
         const uint32_t m = L.size - 1u;
@@ -110,7 +111,8 @@ __device__ __forceinline__ void level_corner_entries(const GridLevel& L, uint32_
         for (int c = 0; c < 8; ++c) e[c] &= m;
     } else {
         const uint32_t dims = f >> kLevelDimsShift;
-        const uint32_t sy = dims > 1 ? L.res : 0u, sz = dims > 2 ? L.res * L.res : 0u;
+        const uint32_t res = f & kLevelResMask;
+        const uint32_t sy = dims > 1 ? res : 0u, sz = dims > 2 ? res * res : 0u;
         const uint32_t y0 = cy * sy, y1 = (cy + 1u) * sy;
         const uint32_t z0 = cz * sz, z1 = (cz + 1u) * sz;
 #pragma unroll
@@ -127,9 +129,11 @@ __device__ __forceinline__ void level_corner_entries(const GridLevel& L, uint32_
 
 // Features of levels [l0, l0 + nl) (nl <= NL) of one grid for one element: f[2i], f[2i+1] are
 // the two features of level l0 + i.  All gathers of the group are issued before any is used.
+// `levels` is the grid's level table (the kernel parameter copy or a shared-memory copy).
 template <int NL>
-__device__ __forceinline__ void grid_group_forward(const GridDesc& g, uint32_t l0, uint32_t nl, const float* __restrict__ table,
-                                                   float px, float py, float pz, float ml_frac, float (&f)[2 * NL]) {
+__device__ __forceinline__ void grid_group_forward(const GridDesc& g, const GridLevel* __restrict__ levels, uint32_t l0, uint32_t nl,
+                                                   const float* __restrict__ table, float px, float py, float pz, float ml_frac,
+                                                   float (&f)[2 * NL]) {
     const float2* __restrict__ t2 = reinterpret_cast<const float2*>(table);
     uint32_t p0, p1, p2;
     hash_primes(g.hash, p0, p1, p2);
@@ -141,7 +145,7 @@ __device__ __forceinline__ void grid_group_forward(const GridDesc& g, uint32_t l
         const uint32_t l = l0 + i;
         on[i] = (uint32_t)i < nl && !grid_level_masked(l, ml_frac, g.n_levels);
         if (on[i]) {
-            const GridLevel L = g.levels[l];
+            const GridLevel L = levels[l];
             float fx, fy, fz;
             uint32_t cx, cy, cz;
             grid_pos_fract(px, L.scale, fx, cx);
@@ -277,6 +281,50 @@ __device__ __forceinline__ void encode_slot_scalar(const Slot& s, const ModelDes
     }
 }
 
+// Row-per-thread encoding of a tile: thread t encodes rows t, t + nthreads, ...  The position and
+// max level of a row are read once; grid levels go NL at a time (NL * 8 gathers in flight) with
+// the level parameters read from `level_tables` (kMaxLevels entries per grid, shared memory).
+template <int NL, typename Store>
+__device__ __forceinline__ void encode_tile_rows(const ModelDesc& d, const GridLevel* level_tables, const float* __restrict__ params,
+                                                 const float* in_s, uint32_t in_ld, const float* __restrict__ ml_gpu, float ml_scalar,
+                                                 uint32_t row0, uint32_t rows, uint32_t tid, uint32_t nthreads, Store& st) {
+    for (uint32_t r = tid; r < rows; r += nthreads) {
+        const float* row = in_s + r * in_ld;
+        const float ml = ml_gpu ? __ldg(ml_gpu + row0 + r) : ml_scalar;
+        for (uint32_t si = 0; si < d.n_slots; ++si) {
+            const Slot& s = d.slots[si];
+            if (s.type == SLOT_GRID) {
+                const float px = row[s.in_begin], py = row[s.in_begin + 1], pz = row[s.in_begin + 2];
+                const GridDesc& g = d.grids[s.grid];
+                const uint32_t nlev = g.n_levels;
+                const float* table = params + g.param_offset;
+                const GridLevel* lv = level_tables + s.grid * kMaxLevels;
+#pragma unroll 1
+                for (uint32_t l0 = 0; l0 < nlev; l0 += NL) {
+                    float f[2 * NL];
+                    const uint32_t nl = min((uint32_t)NL, nlev - l0);
+                    grid_group_forward<NL>(g, lv, l0, nl, table, px, py, pz, ml, f);
+                    st.run(r, s.out_begin + 2u * l0, f, 2u * nl);
+                }
+                if (s.n_pad) encode_slot_scalar(s, d, row, [&](uint32_t col, float v) { st.one(r, col, v); });
+            } else if (s.type == SLOT_SH && s.degree == 4 && s.n_pad == 0 && (s.out_begin & 1u) == 0) {
+                float v[16];
+                sh_forward(4u, row[s.in_begin], row[s.in_begin + 1], row[s.in_begin + 2], [&](uint32_t i, float x) { v[i] = x; });
+                st.run(r, s.out_begin, v, 16u);
+            } else if (s.type == SLOT_ONEHOT && s.out_width <= 16u && (s.out_width & 1u) == 0 && (s.out_begin & 1u) == 0) {
+                float v[16];
+                int bin = (int)floorf(row[s.in_begin] * (float)s.n_bins);
+                bin = bin < 0 ? 0 : (bin >= (int)s.n_bins ? (int)s.n_bins - 1 : bin);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = j == bin ? 1.0f : 0.0f;
+                st.run(r, s.out_begin, v, s.out_width);
+            } else {
+                encode_slot_scalar(s, d, row, [&](uint32_t col, float v) { st.one(r, col, v); });
+            }
+        }
+    }
+}
+
 // Encodes `rows` staged input rows (in_s, row stride in_ld) into the consumer's tile; each grid
 // unit covers NL levels (NL = 2 or 4).
 // Store must provide: run(r, col, const float (&f)[2*NL], n) storing f[0..n) at columns
@@ -298,7 +346,7 @@ __device__ __forceinline__ void encode_tile(const ModelDesc& d, const float* __r
             const uint32_t l0 = grp * NL;
             const uint32_t nl = min((uint32_t)NL, g.n_levels - l0);
             float f[2 * NL];
-            grid_group_forward<NL>(g, l0, nl, table, row[0], row[1], row[2], ml, f);
+            grid_group_forward<NL>(g, g.levels, l0, nl, table, row[0], row[1], row[2], ml, f);
             st.run(r, s.out_begin + 2u * l0, f, 2u * nl);
         }
     }

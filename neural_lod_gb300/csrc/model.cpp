@@ -172,9 +172,9 @@ void build_grid(const Json& j, uint32_t n_dims, EncNode& n) {
         in_level = next_multiple(in_level, 8u);
         if (g.kind == GRID_TILED) in_level = std::min(in_level, powi_u(base_res, 3));
         else if (g.kind == GRID_HASH) in_level = std::min(in_level, 1u << log2T);
+        if (res > kLevelResMask) throw std::runtime_error("GridEncoding: level resolution must be below 2^28");
         g.levels[i].offset = offset;
         g.levels[i].size = in_level;
-        g.levels[i].res = res;
         g.levels[i].scale = scale;
         // grid_index's loop (grid.h:175-186): dims are folded while the running stride fits.
         uint32_t dims = 0;
@@ -186,7 +186,7 @@ void build_grid(const Json& j, uint32_t n_dims, EncNode& n) {
         uint32_t flags = dims << kLevelDimsShift;
         if (g.kind == GRID_HASH && in_level < stride32) flags |= kLevelHashed;
         if ((in_level & (in_level - 1)) == 0) flags |= kLevelPow2;
-        g.levels[i].flags = flags;
+        g.levels[i].res_flags = res | flags;
         if ((uint64_t)offset + in_level > 0x7FFFFFFFull) throw std::runtime_error("GridEncoding: too many parameters");
         offset += in_level;
     }

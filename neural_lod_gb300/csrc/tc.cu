@@ -45,6 +45,7 @@ struct TcLayout {
     uint32_t in_rel;              // staged input rows (FP32), relative to the region
     uint32_t in_ld;
     uint32_t group_stride;
+    uint32_t lvl_off;             // grid level tables (kMaxGrids x kMaxLevels GridLevel)
     uint32_t bar_off;             // G mbarriers, then the TMEM base address
     uint32_t total;
     uint32_t tmem_cols;           // G * width rounded up to a power of two
@@ -62,6 +63,8 @@ __host__ __device__ inline TcLayout tc_layout(const ModelDesc& d, int G) {
     L.in_rel = align_up(L.a_bytes, 128);
     L.group_stride = L.in_rel + align_up(kTcTile * L.in_ld * 4u, 128);
     off += (uint32_t)G * L.group_stride;
+    L.lvl_off = off;
+    off += kMaxGrids * kMaxLevels * (uint32_t)sizeof(GridLevel);
     L.bar_off = off;
     off += 8 * G + 8;
     L.total = align_up(off, 128);
@@ -174,6 +177,11 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
             }
         }
     }
+    GridLevel* lvl_s = reinterpret_cast<GridLevel*>(smem + L.lvl_off);
+    for (uint32_t i = tid; i < d.n_grids * (uint32_t)kMaxLevels; i += kThreads) {
+        const uint32_t g = i / kMaxLevels, l = i % kMaxLevels;
+        if (l < d.grids[g].n_levels) lvl_s[i] = d.grids[g].levels[l];
+    }
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
     __syncthreads();
@@ -202,7 +210,7 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
         // 2. encoding into the A operand (K = enc_width)
         {
             TcStore<T> st{a_tile, d.enc_width * 16u};
-            encode_tile<NL>(d, a.params, in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile, gtid, kGroupThreads, st);
+            encode_tile_rows<NL>(d, lvl_s, a.params, in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile, gtid, kGroupThreads, st);
         }
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
@@ -225,9 +233,10 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
                 }
                 tc::mma_commit(bar);
             }
-            const bool ok = tc::mbar_wait_bounded(bar, phase, kWaitCycles);
+            // Only the issuing thread polls the mbarrier; the rest of the group sleeps in the
+            // named barrier instead of burning issue slots the other groups need.
+            const bool ok = gtid != 0 || tc::mbar_wait_bounded(bar, phase, kWaitCycles);
             phase ^= 1u;
-            // Uniform decision within the group: every thread has finished its bounded wait.
             if (group_sync_or(bar_id, !ok)) { aborted = true; break; }
             tc::fence_after_sync();
 
