@@ -151,6 +151,22 @@ NLOD_API void nlod_ctx_destroy(nlod_ctx* ctx);
 NLOD_API int nlod_training_step(nlod_module* m, void* stream, uint32_t n, const float* in,
                        const float* target, float* loss_out);
 
+/*
+ * nlod_training_step for callers that cannot allocate device memory while they train, for example
+ * an online learner that takes one step inside a real-time frame loop with a no-allocation budget.
+ * No counterpart in the reference (tiny-cuda-nn's Trainer allocates its step workspace from its
+ * memory arena).  Same arguments, result and status codes as nlod_training_step; the step's
+ * intermediates live in a fixed 16 MiB device scratch that the library holds on every GPU that uses
+ * it until the process exits, instead of a cudaMalloc'ed workspace, and the call itself allocates
+ * nothing.  A batch whose intermediates do not fit is rejected with NLOD_ERR_INVALID and a message
+ * giving the largest batch this network can use (about 10k elements for a 48-wide encoding with two
+ * 64-wide hidden layers).  The first call on a device looks up the scratch's device address for that
+ * device; make that first call before any stream capture.  All calls share the one scratch, so calls
+ * that overlap on the GPU (other streams or threads) race on it.
+ */
+NLOD_API int nlod_training_step_noalloc(nlod_module* m, void* stream, uint32_t n, const float* in,
+                                        const float* target, float* loss_out);
+
 /* Same as nlod_training_step without the optimizer step (run_optimizer = false). */
 NLOD_API int nlod_forward_backward_loss(nlod_module* m, void* stream, uint32_t n, const float* in,
                                const float* target, float* loss_out);

@@ -47,6 +47,7 @@ SIGNATURES = [
     ("nlod_ctx_destroy", None, [_vp]),
     ("nlod_training_step", C.c_int, [_vp, _vp, _u32, _fp, _fp, _fp]),
     ("nlod_forward_backward_loss", C.c_int, [_vp, _vp, _u32, _fp, _fp, _fp]),
+    ("nlod_training_step_noalloc", C.c_int, [_vp, _vp, _u32, _fp, _fp, _fp]),
     ("nlod_optimizer_step", C.c_int, [_vp, _vp]),
     ("nlod_optimizer_step_count", _u32, [_vp]),
     ("nlod_learning_rate", C.c_float, [_vp]),

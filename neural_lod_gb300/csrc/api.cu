@@ -548,6 +548,104 @@ int nlod_forward_backward_loss(nlod_module* m, void* stream, uint32_t n, const f
     return train_impl(m, stream, n, in, target, loss_out, false);
 }
 
+// Scratch plan of nlod_training_step_noalloc: the workspace buffers of one step, each 256-byte
+// aligned, followed by the per-block loss partial sums.
+struct NoAllocPlan {
+    size_t enc, hidden, y, dz, delta, d_enc, partial, total;
+};
+
+static NoAllocPlan noalloc_plan(const ModelDesc& d, uint32_t n) {
+    auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+    NoAllocPlan p{};
+    size_t off = 0;
+    p.enc = off;     off += al(sizeof(float) * (size_t)n * d.enc_width);
+    p.hidden = off;  off += al(sizeof(float) * (size_t)n * d.width * d.n_hidden_layers);
+    p.y = off;       off += al(sizeof(float) * (size_t)n * 16);
+    p.dz = off;      off += al(sizeof(float) * (size_t)n * 16);
+    p.delta = off;   off += al(sizeof(float) * (size_t)n * d.width * d.n_hidden_layers);
+    p.d_enc = off;   off += al(sizeof(float) * (size_t)n * d.enc_width);
+    p.partial = off; off += al(sizeof(float) * 4096);
+    p.total = off;
+    return p;
+}
+
+int nlod_training_step_noalloc(nlod_module* m, void* stream, uint32_t n, const float* in, const float* target, float* loss_out) {
+    return guarded([&] {
+        if (!m) throw Error(NLOD_ERR_INVALID, "module is NULL");
+        if (!m->has_loss) throw Error(NLOD_ERR_STATE, "module was created without a loss");
+        if (!m->has_opt) throw Error(NLOD_ERR_STATE, "module was created without an optimizer");
+        check_batch(n);
+        if (n == 0) throw Error(NLOD_ERR_INVALID, "empty batch");
+        if (!in || !target) throw Error(NLOD_ERR_INVALID, "input and target must not be NULL");
+        const ModelDesc& d = m->d;
+        const NoAllocPlan plan = noalloc_plan(d, n);
+        if (plan.total > kNoAllocScratchBytes) {
+            uint32_t max_n = 0;
+            for (uint32_t k = 128; noalloc_plan(d, k).total <= kNoAllocScratchBytes; k += 128) max_n = k;
+            throw Error(NLOD_ERR_INVALID, "batch of " + std::to_string(n) + " needs " + std::to_string(plan.total) +
+                                              " bytes of scratch; the no-allocation training step has a fixed 16 MiB scratch, "
+                                              "which holds at most " + std::to_string(max_n) + " elements for this network");
+        }
+        void* base = nullptr;
+        size_t cap = 0;
+        cuda_check(noalloc_scratch(&base, &cap), "no-allocation scratch address");
+        unsigned char* b = static_cast<unsigned char*>(base);
+        float* enc = reinterpret_cast<float*>(b + plan.enc);
+        float* hidden = reinterpret_cast<float*>(b + plan.hidden);
+        float* y = reinterpret_cast<float*>(b + plan.y);
+        float* dz = reinterpret_cast<float*>(b + plan.dz);
+        float* delta = reinterpret_cast<float*>(b + plan.delta);
+        float* d_enc = reinterpret_cast<float*>(b + plan.d_enc);
+        float* partial = reinterpret_cast<float*>(b + plan.partial);
+        cudaStream_t s = (cudaStream_t)stream;
+        const float loss_scale = 128.0f;
+        // The partial sums are reduced over all 4096 slots: they must start at zero.
+        cuda_check(cudaMemsetAsync(partial, 0, sizeof(float) * 4096, s), "memset");
+        ForwardArgs a = base_forward_args(m, n, in, false);
+        a.enc = enc;
+        a.hidden = hidden;
+        a.y = y;
+        a.loss_kind = m->loss.kind;
+        a.target = target;
+        a.loss_scale = loss_scale;
+        a.dz = dz;
+        a.loss_partial = partial;
+        int blocks = forward_simt_blocks(d);
+        if (blocks > 4096) blocks = 4096;
+        cuda_check(launch_forward_simt(d, a, blocks, s), "forward");
+        if (loss_out) cuda_check(launch_reduce_sum(partial, 4096, loss_out, 1.0f, s), "loss");
+        cuda_check(cudaMemsetAsync(m->grads, 0, sizeof(float) * (size_t)m->n_params, s), "memset grads");
+        BackwardArgs bw{};
+        bw.n = n;
+        bw.params = m->params;
+        bw.hidden = hidden;
+        bw.dz = dz;
+        bw.delta = delta;
+        bw.d_enc = d_enc;
+        cuda_check(launch_backward_delta_simt(d, bw, s), "backward delta");
+        WeightGradArgs wg{};
+        wg.n = n;
+        wg.enc = enc;
+        wg.hidden = hidden;
+        wg.delta = delta;
+        wg.dz = dz;
+        wg.grads = m->grads;
+        cuda_check(launch_weight_grad_simt(d, wg, s), "weight gradients");
+        if (d.n_grids) {
+            GridBackwardArgs g{};
+            g.n = n;
+            g.in = in;
+            g.d_enc = d_enc;
+            g.max_level_gpu = m->max_level_gpu;
+            g.max_level = m->max_level;
+            g.grads = m->grads;
+            cuda_check(launch_grid_backward(d, g, s), "grid backward");
+        }
+        m->grad_scale = loss_scale;
+        run_optimizer(m, s);
+    });
+}
+
 int nlod_optimizer_step(nlod_module* m, void* stream) {
     return guarded([&] {
         if (!m) throw Error(NLOD_ERR_INVALID, "module is NULL");

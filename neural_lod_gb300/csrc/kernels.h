@@ -99,6 +99,10 @@ struct AdamStepArgs {
 };
 cudaError_t launch_adam_step(const AdamStepArgs& a, cudaStream_t s);
 
+// Fixed scratch of the training step that allocates nothing (noalloc.cu): 16 MiB.
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
+cudaError_t noalloc_scratch(void** ptr, size_t* bytes);
+
 // Tensor-core (tcgen05) forms.  kind 1 = FP16, 2 = BF16.  `variant` selects the CTA
 // organisation (tile pipelines per CTA, grid levels per gather unit); see tc.cu.
 bool tc_supported(const ModelDesc& d);
