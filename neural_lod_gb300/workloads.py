@@ -67,6 +67,38 @@ WORKLOADS = {
 }
 
 
+def pack_bits(occ: np.ndarray) -> np.ndarray:
+    """[res,res,res] bool indexed [z,y,x] -> uint32 words, bit x + y*res + z*res^2, most
+    significant bit first (the cuda_voxelizer grid layout, rptr voxelize.cu:50-55)."""
+    flat = np.ascontiguousarray(occ, dtype=bool).reshape(-1)
+    pad = (-flat.size) % 32
+    if pad:
+        flat = np.concatenate([flat, np.zeros(pad, bool)])
+    return np.packbits(flat.reshape(-1, 32), axis=1, bitorder="big").view(">u4").reshape(-1).astype(np.uint32)
+
+
+def unpack_bits(words: np.ndarray, res: int) -> np.ndarray:
+    b = np.unpackbits(np.asarray(words, dtype=np.uint32).astype(">u4").view(np.uint8), bitorder="big")
+    return b[: res ** 3].astype(bool).reshape(res, res, res)
+
+
+def value_noise_occupancy(res: int, seed: int = 0, spacing: int = 16, density: float = 0.3) -> np.ndarray:
+    """Seeded occupancy [z,y,x]: a lattice of U[0,1] values every `spacing` voxels, trilinearly
+    interpolated at voxel centres and thresholded so that `density` of the voxels are occupied."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = res // spacing + 2
+    lat = rng.random((n, n, n))
+    c = (np.arange(res) + 0.5) / spacing
+    i0 = np.floor(c).astype(np.int64)
+    f = c - i0
+    # separable trilinear interpolation along x, then y, then z
+    a = lat[:, :, i0] * (1 - f) + lat[:, :, i0 + 1] * f
+    a = a[:, i0, :] * (1 - f)[None, :, None] + a[:, i0 + 1, :] * f[None, :, None]
+    a = a[i0, :, :] * (1 - f)[:, None, None] + a[i0 + 1, :, :] * f[:, None, None]
+    thr = np.quantile(a, 1.0 - density)
+    return a > thr
+
+
 def _unit_dirs(rng: np.random.Generator, n: int) -> np.ndarray:
     v = rng.standard_normal((n, 3))
     v /= np.linalg.norm(v, axis=1, keepdims=True)

@@ -70,6 +70,10 @@ def declare(L):
     L.orc_adam_step.argtypes = [vp, i64, i64, vp, vp, vp, vp, vp, vp, f32, f32, f32]
     L.orc_forward_f32.restype = ci
     L.orc_forward_f32.argtypes = [vp, i64, vp, vp, vp, f32, vp, ci]
+    L.orc_lod_level.restype = None
+    L.orc_lod_level.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp, vp]
+    L.orc_first_active_voxel_batch.restype = None
+    L.orc_first_active_voxel_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, vp]
     return L
 
 
@@ -186,10 +190,51 @@ def adam_step(hp: dict, params, grads, m1, m2, steps, n_matrix, loss_scale=1.0, 
                         _p(steps), _p(ema), C.c_float(ema_decay), C.c_float(ema_debias_old), C.c_float(ema_debias_new))
 
 
+class OrcLodLevel(C.Structure):
+    _fields_ = [("res", C.c_int32), ("n_active", C.c_int32), ("bbox_min", C.c_int32 * 3), ("bbox_max", C.c_int32 * 3),
+                ("bits", C.c_void_p), ("leaf", C.c_void_p), ("lower", C.c_void_p)]
+
+
+class LodLevel:
+    """One level of the LoD occupancy pyramid (level-0 voxels >> lod), with the NanoVDB-style leaf
+    (8^3) and lower-node (128^3) existence flags the first-active-voxel search needs."""
+
+    def __init__(self, bits0: np.ndarray, res0: int, lod: int):
+        r = res0 >> lod
+        self.bits = np.zeros(((r ** 3) + 31) // 32, dtype=np.uint32)
+        nb, nl = (r + 7) // 8, (r + 127) // 128
+        self.leaf = np.zeros(nb ** 3, dtype=np.uint8)
+        self.lower = np.zeros(nl ** 3, dtype=np.uint8)
+        self.s = OrcLodLevel()
+        b0 = np.ascontiguousarray(bits0, dtype=np.uint32)
+        lib().orc_lod_level(b0.ctypes.data, res0, lod, self.bits.ctypes.data, self.leaf.ctypes.data,
+                            self.lower.ctypes.data, C.byref(self.s))
+        self.res = r
+
+    @property
+    def bbox(self):
+        return tuple(self.s.bbox_min), tuple(self.s.bbox_max)
+
+    def first_active_voxel(self, eye, dir, t_min=None, prev=None):
+        """Batch search; returns (hit [n] int32, ijk [n,3] int32, t_near [n], t_far [n])."""
+        eye = np.ascontiguousarray(eye, dtype=np.float32)
+        d = np.ascontiguousarray(dir, dtype=np.float32)
+        n = eye.shape[0]
+        tm = None if t_min is None else np.ascontiguousarray(t_min, dtype=np.float32)
+        pv = None if prev is None else np.ascontiguousarray(prev, dtype=np.int32)
+        hit = np.empty(n, np.int32)
+        ijk = np.empty((n, 3), np.int32)
+        tn = np.empty(n, np.float32)
+        tf = np.empty(n, np.float32)
+        lib().orc_first_active_voxel_batch(C.byref(self.s), n, eye.ctypes.data, d.ctypes.data, _p(tm), _p(pv),
+                                           hit.ctypes.data, ijk.ctypes.data, tn.ctypes.data, tf.ctypes.data)
+        return hit, ijk, tn, tf
+
+
 def sh(degree: int, x: float, y: float, z: float):
     out = (C.c_double * (degree * degree))()
     lib().orc_sh(C.c_int(degree), C.c_double(x), C.c_double(y), C.c_double(z), out)
     return np.array(out[:], dtype=np.float64)
 
 
-__all__ = ["Oracle", "adam_step", "sh", "grid_levels", "model_spec"]
+__all__ = ["Oracle", "LodLevel", "adam_step", "sh", "grid_levels", "model_spec"]

@@ -473,3 +473,219 @@ int orc_forward_f32(const OrcModel* m, int64_t n, const float* in, const float* 
     }
     return used;
 }
+
+/* ---------------------------------------------------------------------------------------------
+ * LoD occupancy pyramid + first active voxel along a ray (see nlod_oracle.h for the sources).
+ * IEEE single precision, one rounding per operation (built with -ffp-contract=off); the ray is
+ * evaluated with fmaf like nanovdb::Ray::operator().
+ * ------------------------------------------------------------------------------------------- */
+#include <float.h>
+
+static int orc_bit(const uint32_t* bits, int64_t idx) { return (bits[idx >> 5] >> (31 - (idx & 31))) & 1u; }
+
+void orc_lod_level(const uint32_t* bits0, int32_t res0, int32_t lod, uint32_t* bits_out, uint8_t* leaf_out,
+                   uint8_t* lower_out, OrcLodLevel* level) {
+    const int32_t r = res0 >> lod;
+    const int64_t n = (int64_t)r * r * r;
+    const int32_t nb = (r + 7) / 8, nl = (r + 127) / 128;
+    memset(bits_out, 0, sizeof(uint32_t) * (size_t)((n + 31) / 32));
+    memset(leaf_out, 0, (size_t)nb * nb * nb);
+    memset(lower_out, 0, (size_t)nl * nl * nl);
+    int32_t bmin[3] = {r, r, r}, bmax[3] = {-1, -1, -1};
+    int32_t count = 0;
+    const int64_t n0 = (int64_t)res0 * res0 * res0;
+    for (int64_t i = 0; i < n0; ++i) {
+        if (!orc_bit(bits0, i)) continue;
+        const int32_t x = (int32_t)(i % res0) >> lod, y = (int32_t)((i / res0) % res0) >> lod, z = (int32_t)(i / ((int64_t)res0 * res0)) >> lod;
+        const int64_t j = x + (int64_t)r * (y + (int64_t)r * z);
+        if (!orc_bit(bits_out, j)) {
+            bits_out[j >> 5] |= 1u << (31 - (j & 31));
+            ++count;
+        }
+        leaf_out[(x >> 3) + nb * ((y >> 3) + nb * (z >> 3))] = 1;
+        lower_out[(x >> 7) + nl * ((y >> 7) + nl * (z >> 7))] = 1;
+        const int32_t c[3] = {x, y, z};
+        for (int k = 0; k < 3; ++k) {
+            if (c[k] < bmin[k]) bmin[k] = c[k];
+            if (c[k] > bmax[k]) bmax[k] = c[k];
+        }
+    }
+    level->res = r;
+    level->n_active = count;
+    for (int k = 0; k < 3; ++k) { level->bbox_min[k] = bmin[k]; level->bbox_max[k] = bmax[k]; }
+    level->bits = bits_out;
+    level->leaf = leaf_out;
+    level->lower = lower_out;
+}
+
+/* getDim of a NanoVDB tree holding exactly the active voxels of `L` (one upper node at the origin):
+ * 4096 outside it, 128 where no lower node exists, 8 where no leaf exists, 1 inside a leaf. */
+static int orc_get_dim(const OrcLodLevel* L, const int32_t ijk[3]) {
+    if (L->n_active == 0) return 4096;
+    for (int k = 0; k < 3; ++k)
+        if (ijk[k] < 0 || ijk[k] >= 4096) return 4096;
+    const int32_t nl = (L->res + 127) / 128, nb = (L->res + 7) / 8;
+    const int32_t lx = ijk[0] >> 7, ly = ijk[1] >> 7, lz = ijk[2] >> 7;
+    if (lx >= nl || ly >= nl || lz >= nl || !L->lower[lx + nl * (ly + nl * lz)]) return 128;
+    const int32_t bx = ijk[0] >> 3, by = ijk[1] >> 3, bz = ijk[2] >> 3;
+    if (bx >= nb || by >= nb || bz >= nb || !L->leaf[bx + nb * (by + nb * bz)]) return 8;
+    return 1;
+}
+
+typedef struct {
+    int32_t dim;
+    float t0, t1;
+    int32_t voxel[3], step[3];
+    float delta[3], next[3];
+} OrcHdda;
+
+static void orc_ray_at(const float E[3], const float D[3], float t, float p[3]) {
+    for (int k = 0; k < 3; ++k) p[k] = fmaf(t, D[k], E[k]);
+}
+
+static void orc_hdda_init(OrcHdda* h, const float E[3], const float D[3], const float inv[3], float t0, float t1, int32_t dim) {
+    h->dim = dim;
+    h->t0 = t0;
+    h->t1 = t1;
+    float pos[3];
+    orc_ray_at(E, D, t0, pos);
+    for (int a = 0; a < 3; ++a) {
+        h->voxel[a] = ((int32_t)floorf(pos[a])) & ~(dim - 1);
+        h->delta[a] = 0.f;
+        if (D[a] == 0.f) {
+            h->next[a] = FLT_MAX;
+            h->step[a] = 0;
+        } else if (inv[a] > 0.f) {
+            h->step[a] = 1;
+            h->next[a] = t0 + ((float)(h->voxel[a] + dim) - pos[a]) * inv[a];
+            h->delta[a] = inv[a];
+        } else {
+            h->step[a] = -1;
+            h->next[a] = t0 + ((float)h->voxel[a] - pos[a]) * inv[a];
+            h->delta[a] = -inv[a];
+        }
+    }
+}
+
+static void orc_hdda_update(OrcHdda* h, const float E[3], const float D[3], const float inv[3], int32_t dim) {
+    if (h->dim == dim) return;
+    h->dim = dim;
+    float pos[3];
+    orc_ray_at(E, D, h->t0, pos);
+    for (int a = 0; a < 3; ++a) {
+        h->voxel[a] = ((int32_t)floorf(pos[a])) & ~(dim - 1);
+        if (h->step[a] == 0) continue;
+        h->next[a] = h->t0 + ((float)h->voxel[a] - pos[a]) * inv[a];
+        if (h->step[a] > 0) h->next[a] += (float)dim * inv[a];
+    }
+}
+
+static int orc_hdda_step(OrcHdda* h) {
+    const float* v = h->next;
+    const int a = (v[0] < v[1] && v[0] < v[2]) ? 0 : (v[1] < v[2] ? 1 : 2);
+    if (h->next[a] <= h->t0) h->next[a] += h->t0 - 0.999999f * h->next[a] + 1.0e-6f;
+    h->t0 = h->next[a];
+    h->next[a] += (float)h->dim * h->delta[a];
+    h->voxel[a] += h->dim * h->step[a];
+    return h->t0 <= h->t1;
+}
+
+static int orc_slab(const float o[3], const float d[3], const int32_t ijk[3], float* near_t, float* far_t) {
+    *near_t = -1e20f;
+    *far_t = 1e20f;
+    for (int i = 0; i < 3; ++i) {
+        const float inv = 1.f / d[i];
+        const float lo = (float)ijk[i], hi = lo + 1.0f;
+        if (d[i] == 0.f) {
+            if (o[i] < lo || o[i] > hi) return 0;
+        } else {
+            float t1 = (lo - o[i]) * inv, t2 = (hi - o[i]) * inv;
+            if (t1 > t2) { const float t = t1; t1 = t2; t2 = t; }
+            *near_t = (t1 < *near_t) ? *near_t : t1;
+            *far_t = (*far_t < t2) ? *far_t : t2;
+            if (!(*near_t < *far_t) || (double)*far_t < 0.0) return 0;
+        }
+    }
+    return 1;
+}
+
+int orc_first_active_voxel(const OrcLodLevel* L, const float E[3], const float D[3], float t_min, const int32_t prev[3],
+                           int32_t ijk_out[3], float* t_near, float* t_far) {
+    if (L->n_active == 0) return 0;
+    const float inv[3] = {1.f / D[0], 1.f / D[1], 1.f / D[2]};
+    /* Ray::clip against the root bbox [min, max + 1) */
+    float t0 = t_min, t1 = FLT_MAX;
+    for (int i = 0; i < 3; ++i) {
+        float a = (float)L->bbox_min[i], b = (float)(L->bbox_max[i] + 1);
+        if (a >= b) return 0;
+        a = (a - E[i]) * inv[i];
+        b = (b - E[i]) * inv[i];
+        if (a > b) { const float t = a; a = b; b = t; }
+        if (a > t0) t0 = a;
+        if (b < t1) t1 = b;
+        if (t0 > t1) return 0;
+    }
+    /* TreeMarcher::init */
+    const float ta = t0 + 0.000001f, tb = t1 - 0.000001f;
+    if (ta > tb) return 0;
+    int32_t ijk[3], leaf[3] = {0, 0, 0};
+    int have_leaf = 0;
+    float p[3];
+    orc_ray_at(E, D, ta, p);
+    for (int k = 0; k < 3; ++k) ijk[k] = (int32_t)floorf(p[k]);
+    int dim = orc_get_dim(L, ijk);
+    if (dim == 1) { have_leaf = 1; for (int k = 0; k < 3; ++k) leaf[k] = ijk[k] >> 3; }
+    OrcHdda h;
+    orc_hdda_init(&h, E, D, inv, ta, tb, dim > 8 ? dim : 8);
+    float mt0 = dim <= 1 ? h.t0 : -1.f;
+    const float tmax = tb;
+    /* TreeMarcher::step loop with the per-leaf DDA search */
+    int valid;
+    do {
+        const float s0 = mt0;
+        const int cur_have = have_leaf;
+        const int32_t cur[3] = {leaf[0], leaf[1], leaf[2]};
+        valid = orc_hdda_step(&h);
+        orc_ray_at(E, D, h.t0 + 0.01f, p);
+        int32_t nxt[3];
+        for (int k = 0; k < 3; ++k) nxt[k] = (int32_t)floorf(p[k]);
+        const int nd = orc_get_dim(L, nxt);
+        if (nd == 1) { have_leaf = 1; for (int k = 0; k < 3; ++k) leaf[k] = nxt[k] >> 3; }
+        orc_hdda_update(&h, E, D, inv, nd > 8 ? nd : 8);
+        mt0 = nd <= 1 ? h.t0 : -1.f;
+        if (s0 >= 0.f) {
+            const float s1 = (tmax < h.t0) ? tmax : h.t0;
+            if (s0 >= s1 || !cur_have) continue;
+            OrcHdda dda;
+            orc_hdda_init(&dda, E, D, inv, s0, s1, 1);
+            do {
+                const int32_t* v = dda.voxel;
+                if (v[0] - cur[0] * 8 < 0 || v[1] - cur[1] * 8 < 0 || v[2] - cur[2] * 8 < 0 || v[0] - cur[0] * 8 >= 8 ||
+                    v[1] - cur[1] * 8 >= 8 || v[2] - cur[2] * 8 >= 8)
+                    continue;
+                if (v[0] >= L->res || v[1] >= L->res || v[2] >= L->res) continue;
+                if (!orc_bit(L->bits, v[0] + (int64_t)L->res * (v[1] + (int64_t)L->res * v[2]))) continue;
+                if (v[0] == prev[0] && v[1] == prev[1] && v[2] == prev[2]) continue;
+                if (orc_slab(E, D, v, t_near, t_far)) {
+                    for (int k = 0; k < 3; ++k) ijk_out[k] = v[k];
+                    return 1;
+                }
+            } while (orc_hdda_step(&dda));
+        }
+    } while (valid);
+    return 0;
+}
+
+void orc_first_active_voxel_batch(const OrcLodLevel* L, int64_t n, const float* eye, const float* dir, const float* t_min,
+                                  const int32_t* prev, int32_t* hit, int32_t* ijk, float* t_near, float* t_far) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; ++i) {
+        const int32_t none[3] = {-1, -1, -1};
+        float tn = 0.f, tf = 0.f;
+        int32_t v[3] = {0, 0, 0};
+        hit[i] = orc_first_active_voxel(L, eye + 3 * i, dir + 3 * i, t_min ? t_min[i] : 0.f, prev ? prev + 3 * i : none, v, &tn, &tf);
+        for (int k = 0; k < 3; ++k) ijk[3 * i + k] = hit[i] ? v[k] : 0;
+        t_near[i] = hit[i] ? tn : 0.f;
+        t_far[i] = hit[i] ? tf : 0.f;
+    }
+}

@@ -106,6 +106,35 @@ void orc_adam_step(const OrcAdam* a, int64_t n_params, int64_t n_matrix, float* 
                    float* m1, float* m2, uint32_t* steps, float* ema, float ema_decay, float ema_debias_old,
                    float ema_debias_new);
 
+/* ---- LoD occupancy pyramid and first-active-voxel search (restating
+ *      rptr/cuda/neural-lod/neural_lod_learning_init.cu:194-267 (pyramid by >> lod),
+ *      rptr/ext/nanovdb/nanovdb/util/HDDA.h:27-188, 190-307, 370-450 (HDDA, DDA, TreeMarcher),
+ *      rptr/ext/nanovdb/nanovdb/util/Ray.h:153-158, 398-424 (ray eval, bbox clip),
+ *      rptr/ext/nanovdb/nanovdb/NanoVDB.h:3358-3369, 3745-3757, 4442-4448 (getDim),
+ *      rptr/cuda/neural-lod/neural_lod_learning_common.cuh:567-606, 783-832 (slab test, search)) */
+typedef struct {
+    int32_t res;            /* voxels per axis */
+    int32_t n_active;
+    int32_t bbox_min[3], bbox_max[3];   /* tight inclusive bbox of active voxels */
+    const uint32_t* bits;   /* occupancy, bit x + y*res + z*res*res, MSB first in each word */
+    const uint8_t* leaf;    /* [ceil(res/8)]^3 flags: 8^3 block has an active voxel */
+    const uint8_t* lower;   /* [ceil(res/128)]^3 flags: 128^3 block has a leaf */
+} OrcLodLevel;
+
+/* Level `lod` of the pyramid from level-0 bits (res0 per axis): voxel (x,y,z) >> lod.
+ * bits_out: ceil((res0>>lod)^3 / 32) words; leaf_out / lower_out sized as above. */
+void orc_lod_level(const uint32_t* bits0, int32_t res0, int32_t lod, uint32_t* bits_out, uint8_t* leaf_out,
+                   uint8_t* lower_out, OrcLodLevel* level);
+
+/* First active voxel along an index-space ray (eye, dir, t_min; t_max = 1e38), skipping `prev`.
+ * Returns 1 and ijk / t_near / t_far on a hit, 0 on a miss. */
+int orc_first_active_voxel(const OrcLodLevel* level, const float eye[3], const float dir[3], float t_min,
+                           const int32_t prev[3], int32_t ijk[3], float* t_near, float* t_far);
+
+void orc_first_active_voxel_batch(const OrcLodLevel* level, int64_t n, const float* eye, const float* dir,
+                                  const float* t_min, const int32_t* prev, int32_t* hit, int32_t* ijk,
+                                  float* t_near, float* t_far);
+
 /* FP32 scalar forward over all host threads: the timed CPU baseline. Returns threads used. */
 int orc_forward_f32(const OrcModel* m, int64_t n, const float* in, const float* params, const float* max_level,
                     float max_level_scalar, float* out, int n_threads);
