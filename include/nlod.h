@@ -211,6 +211,37 @@ NLOD_API int nlod_get_kernel_variant(const nlod_module* m);
 NLOD_API int nlod_set_kernel_variant(nlod_module* m, int variant);
 NLOD_API int nlod_autotune(nlod_module* m, void* stream, uint32_t n, const float* in, float* out);
 
+/* ---- LoD occupancy pyramid and first-active-voxel search ----------------------------------
+ * The reference builds one NanoVDB grid per LoD from the voxelizer's point cloud, level k holding
+ * voxel (x,y,z) >> k (rptr/cuda/neural-lod/neural_lod_learning_init.cu:194-267), and marches
+ * index-space rays through it with nanovdb::TreeMarcher + DDA in first_active_voxel_intersection
+ * (rptr/cuda/neural-lod/neural_lod_learning_common.cuh:783-832), called from raymarch_impl
+ * (rptr/cuda/wavefront_neural_pt.cuh:89-141).  Here the pyramid is a bit-packed grid per level
+ * (bit x + y*res + z*res^2, most significant bit first per uint32: the cuda_voxelizer output) and
+ * the search returns the same voxel, t_near and t_far as NanoVDB's DDA in IEEE single precision. */
+typedef struct nlod_lod_grid nlod_lod_grid;
+
+/* Builds n_levels levels from a level-0 occupancy of res^3 voxels (device buffer, copied).
+ * res must be a power of two <= 4096.  Synchronous. */
+NLOD_API int nlod_lod_grid_create(const uint32_t* level0_bits, uint32_t res, uint32_t n_levels, void* stream,
+                                  nlod_lod_grid** out);
+NLOD_API void nlod_lod_grid_destroy(nlod_lod_grid* g);
+/* Resolution, active voxel count, tight bbox (min xyz, max xyz) and NanoVDB leaf-node count. */
+NLOD_API int nlod_lod_grid_level_info(const nlod_lod_grid* g, uint32_t level, int32_t* res, int32_t* n_active,
+                                      int32_t* bbox6, uint32_t* n_leaves);
+/* Device pointer to a level's occupancy bits (owned by the grid). */
+NLOD_API const uint32_t* nlod_lod_grid_level_bits(const nlod_lod_grid* g, uint32_t level);
+/* Copies a level's occupancy words (ceil(res^3/32) uint32) to host memory.  Synchronous. */
+NLOD_API int nlod_lod_grid_copy_bits(const nlod_lod_grid* g, uint32_t level, uint32_t* host_dst);
+/* For n index-space rays (origin, dir: [n][3]; t_min: [n] or NULL for 0; prev: [n][3] voxel to skip
+ * or NULL for none) writes hit [n] (0/1), ijk [n][3], t_near [n], t_far [n] of the first active
+ * voxel of `level` (first_active_voxel_intersection).  Asynchronous. */
+NLOD_API int nlod_first_active_voxel(const nlod_lod_grid* g, uint32_t level, void* stream, uint32_t n,
+                                     const float* origin, const float* dir, const float* t_min, const int32_t* prev,
+                                     int32_t* hit, int32_t* ijk, float* t_near, float* t_far);
+/* NLOD_ERR_TIMEOUT if a ray of an earlier search exceeded its step budget (reported as a miss). */
+NLOD_API int nlod_lod_grid_sync_status(nlod_lod_grid* g, void* stream);
+
 /* Device status word of the last launch sequence (NLOD_OK or NLOD_ERR_TIMEOUT); synchronises. */
 NLOD_API int nlod_sync_status(nlod_module* m, void* stream);
 

@@ -62,6 +62,13 @@ SIGNATURES = [
     ("nlod_set_kernel_variant", C.c_int, [_vp, C.c_int]),
     ("nlod_autotune", C.c_int, [_vp, _vp, _u32, _fp, _fp]),
     ("nlod_sync_status", C.c_int, [_vp, _vp]),
+    ("nlod_lod_grid_create", C.c_int, [_fp, _u32, _u32, _vp, C.POINTER(_vp)]),
+    ("nlod_lod_grid_destroy", None, [_vp]),
+    ("nlod_lod_grid_level_info", C.c_int, [_vp, _u32, _fp, _fp, _fp, _fp]),
+    ("nlod_lod_grid_level_bits", C.c_void_p, [_vp, _u32]),
+    ("nlod_lod_grid_copy_bits", C.c_int, [_vp, _u32, _fp]),
+    ("nlod_first_active_voxel", C.c_int, [_vp, _u32, _vp, _u32, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]),
+    ("nlod_lod_grid_sync_status", C.c_int, [_vp, _vp]),
 ]
 
 _lib = None

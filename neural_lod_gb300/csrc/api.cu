@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "nlod.h"
+#include "abi_util.h"
 #include "desc.h"
 #include "json.h"
 #include "kernels.h"
@@ -23,51 +24,12 @@
 using namespace nlod;
 
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
 
-struct Error : std::runtime_error {
-    int code;
-    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
-};
+std::string& nlod::last_error() { return g_last_error; }
 
-void cuda_check(cudaError_t e, const char* what) {
-    if (e != cudaSuccess) {
-        cudaGetLastError();  // clear non-sticky errors
-        throw Error(e == cudaErrorMemoryAllocation ? NLOD_ERR_ALLOC : NLOD_ERR_CUDA,
-                    std::string(what) + ": " + cudaGetErrorString(e));
-    }
-}
-
-template <typename T>
-T* dev_alloc(size_t count) {
-    if (count == 0) return nullptr;
-    void* p = nullptr;
-    cuda_check(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
-    return static_cast<T*>(p);
-}
-
-void dev_free(void* p) {
-    if (p) cudaFree(p);
-}
-
-template <typename F>
-int guarded(F&& f) {
-    try {
-        f();
-        g_last_error.clear();
-        return NLOD_OK;
-    } catch (const Error& e) {
-        g_last_error = e.what();
-        return e.code;
-    } catch (const std::bad_alloc&) {
-        g_last_error = "host allocation failed";
-        return NLOD_ERR_ALLOC;
-    } catch (const std::exception& e) {
-        g_last_error = e.what();
-        return NLOD_ERR_INVALID;
-    }
-}
+namespace {
 
 // Growable device workspace for training-mode forward/backward intermediates.
 struct Workspace {
