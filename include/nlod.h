@@ -245,6 +245,28 @@ NLOD_API int nlod_lod_grid_sync_status(nlod_lod_grid* g, void* stream);
 /* Device status word of the last launch sequence (NLOD_OK or NLOD_ERR_TIMEOUT); synchronises. */
 NLOD_API int nlod_sync_status(nlod_module* m, void* stream);
 
+/* ---- Conservative surface voxelization --------------------------------------------------------
+ * The reference's cuda_voxelizer (run as `cuda_voxelizer -f mesh -s G -o obj_points -pad` by
+ * results/scripts/voxelize.py:36): main.cpp:204-257 takes the trimesh bbox, cubes and pads it with
+ * createMeshBBCube (util.h:87-112, epsilonPadding 1e-4, main.cpp:45) and launches voxelize_triangle
+ * (voxelize.cu:58-190), which ORs bit x + y*G + z*G^2 (most significant bit first per uint32,
+ * setBit voxelize.cu:50-55) for every voxel whose closed box overlaps a triangle.  Triangles are a
+ * soup of n x 9 floats (v0 v1 v2, xyz each), like meshToGPU_thrust's buffer. */
+
+/* Per-axis min / max of all vertices of n device triangles (trimesh's need_bbox). Synchronous. */
+NLOD_API int nlod_mesh_bounds(const float* triangles, uint64_t n_triangles, void* stream, float mesh_min[3],
+                              float mesh_max[3]);
+/* createMeshBBCube + voxinfo on the host: the cube frame around [mesh_min, mesh_max] padded by
+ * epsilon_padding * extent per side (0 for none), and the voxel size (bbox_max - bbox_min) / grid. */
+NLOD_API int nlod_mesh_frame(const float mesh_min[3], const float mesh_max[3], uint32_t grid, float epsilon_padding,
+                             float bbox_min[3], float bbox_max[3], float unit[3]);
+/* ORs the conservative surface voxelization of n device triangles into `bits` (device,
+ * ceil(grid^3 / 32) uint32 words, zeroed by the caller for a fresh grid); grid <= 4096.  The
+ * voxel set equals voxelize_triangle's evaluated in IEEE single precision without contraction.
+ * Asynchronous on `stream`. */
+NLOD_API int nlod_voxelize(const float* triangles, uint64_t n_triangles, uint32_t grid, const float bbox_min[3],
+                           const float unit[3], uint32_t* bits, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,6 +69,9 @@ SIGNATURES = [
     ("nlod_lod_grid_copy_bits", C.c_int, [_vp, _u32, _fp]),
     ("nlod_first_active_voxel", C.c_int, [_vp, _u32, _vp, _u32, _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]),
     ("nlod_lod_grid_sync_status", C.c_int, [_vp, _vp]),
+    ("nlod_mesh_bounds", C.c_int, [_fp, C.c_uint64, _vp, _fp, _fp]),
+    ("nlod_mesh_frame", C.c_int, [_fp, _fp, _u32, C.c_float, _fp, _fp, _fp]),
+    ("nlod_voxelize", C.c_int, [_fp, C.c_uint64, _u32, _fp, _fp, _fp, _vp]),
 ]
 
 _lib = None

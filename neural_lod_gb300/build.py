@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-    "-Xcompiler", "-Wall", "-I", str(INCLUDE), "-I", str(CSRC),
+    "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off", "-I", str(INCLUDE), "-I", str(CSRC),
 ]
 
 

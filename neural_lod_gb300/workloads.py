@@ -151,3 +151,56 @@ def test_params(spec: dict, seed: int = 7, grid_scale: float = 0.5) -> np.ndarra
     n_net = spec["n_params_network"]
     p[n_net:] = rng.uniform(-grid_scale, grid_scale, spec["n_params"] - n_net)
     return p
+
+
+def _rotations(rng: np.random.Generator, n: int) -> np.ndarray:
+    """n random rotation matrices [n,3,3] (QR of Gaussian matrices, sign-fixed)."""
+    q, r = np.linalg.qr(rng.standard_normal((n, 3, 3)))
+    q *= np.sign(np.diagonal(r, axis1=1, axis2=2))[:, None, :]
+    return q
+
+
+def ellipsoid_shells(n: int, seed: int = 0, slices: int = 8, stacks: int = 4, radius=(0.004, 0.02)) -> np.ndarray:
+    """n randomly placed, oriented and scaled ellipsoid shells inside the unit cube, each a UV
+    sphere of 2*slices*(stacks-1) triangles.  Returns float32 [n*tris, 9]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    th = np.pi * np.arange(1, stacks) / stacks
+    ph = 2 * np.pi * np.arange(slices) / slices
+    ring = np.stack([np.sin(th)[:, None] * np.cos(ph)[None], np.sin(th)[:, None] * np.sin(ph)[None],
+                     np.broadcast_to(np.cos(th)[:, None], (stacks - 1, slices))], -1).reshape(-1, 3)
+    verts = np.concatenate([[[0, 0, 1]], ring, [[0, 0, -1]]])            # [2 + slices*(stacks-1), 3]
+    top, bot = 0, len(verts) - 1
+    idx = lambda s, j: 1 + s * slices + (j % slices)
+    tri = [(top, idx(0, j), idx(0, j + 1)) for j in range(slices)]
+    for s in range(stacks - 2):
+        for j in range(slices):
+            tri += [(idx(s, j), idx(s + 1, j), idx(s + 1, j + 1)), (idx(s, j), idx(s + 1, j + 1), idx(s, j + 1))]
+    tri += [(idx(stacks - 2, j), bot, idx(stacks - 2, j + 1)) for j in range(slices)]
+    tri = np.asarray(tri)
+    radii = rng.uniform(radius[0], radius[1], (n, 3))
+    centre = rng.uniform(radius[1], 1 - radius[1], (n, 3))
+    rot = _rotations(rng, n)
+    local = verts[None, :, :] * radii[:, None, :]                          # [n, V, 3]
+    world = np.einsum("nij,nvj->nvi", rot, local) + centre[:, None, :]
+    return world[:, tri, :].reshape(-1, 9).astype(np.float32)
+
+
+def foliage_quads(n: int, seed: int = 1, side=(1e-3, 1e-2)) -> np.ndarray:
+    """n randomly oriented rectangles with sides U[side] inside the unit cube, two triangles each.
+    Returns float32 [2n, 9]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    rot = _rotations(rng, n)
+    a = rng.uniform(side[0], side[1], (n, 1)) * rot[:, :, 0]
+    b = rng.uniform(side[0], side[1], (n, 1)) * rot[:, :, 1]
+    m = side[1]
+    c = rng.uniform(m, 1 - m, (n, 3))
+    p00, p10, p11, p01 = c - (a + b) / 2, c + (a - b) / 2, c + (a + b) / 2, c + (b - a) / 2
+    t = np.stack([np.concatenate([p00, p10, p11], 1), np.concatenate([p00, p11, p01], 1)], 1)
+    return t.reshape(-1, 9).astype(np.float32)
+
+
+def synthetic_mesh(n_ellipsoids: int = 20_000, n_quads: int = 520_000, seed: int = 0) -> np.ndarray:
+    """The voxelize+train scene: ellipsoid shells (48 triangles each) plus foliage-like quads in the
+    unit cube; defaults give 20k shells + 0.52M quads = 2.0M triangles.  float32 [n, 9]."""
+    parts = [ellipsoid_shells(n_ellipsoids, seed=seed), foliage_quads(n_quads, seed=seed + 1)]
+    return np.concatenate(parts, 0)

@@ -74,6 +74,10 @@ def declare(L):
     L.orc_lod_level.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp, vp]
     L.orc_first_active_voxel_batch.restype = None
     L.orc_first_active_voxel_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.orc_mesh_frame.restype = None
+    L.orc_mesh_frame.argtypes = [vp, vp, C.c_uint32, f32, vp, vp, vp]
+    L.orc_voxelize.restype = None
+    L.orc_voxelize.argtypes = [vp, i64, vp, vp, C.c_uint32, vp]
     return L
 
 
@@ -231,10 +235,31 @@ class LodLevel:
         return hit, ijk, tn, tf
 
 
+def mesh_frame(mesh_min, mesh_max, grid: int, eps: float = 1e-4):
+    """createMeshBBCube + voxinfo: (bbox_min, bbox_max, unit), each float32[3]."""
+    mn = np.ascontiguousarray(mesh_min, dtype=np.float32)
+    mx = np.ascontiguousarray(mesh_max, dtype=np.float32)
+    bmin, bmax, unit = (np.zeros(3, np.float32) for _ in range(3))
+    lib().orc_mesh_frame(mn.ctypes.data, mx.ctypes.data, grid, C.c_float(eps), bmin.ctypes.data, bmax.ctypes.data,
+                         unit.ctypes.data)
+    return bmin, bmax, unit
+
+
+def voxelize(triangles, grid: int, bbox_min, unit, bits=None):
+    """Conservative surface voxelization (voxelize_triangle); returns the grid^3 bit words."""
+    t = np.ascontiguousarray(triangles, dtype=np.float32).reshape(-1, 9)
+    if bits is None:
+        bits = np.zeros((grid ** 3 + 31) // 32, dtype=np.uint32)
+    bmin = np.ascontiguousarray(bbox_min, dtype=np.float32)
+    u = np.ascontiguousarray(unit, dtype=np.float32)
+    lib().orc_voxelize(t.ctypes.data, t.shape[0], bmin.ctypes.data, u.ctypes.data, grid, bits.ctypes.data)
+    return bits
+
+
 def sh(degree: int, x: float, y: float, z: float):
     out = (C.c_double * (degree * degree))()
     lib().orc_sh(C.c_int(degree), C.c_double(x), C.c_double(y), C.c_double(z), out)
     return np.array(out[:], dtype=np.float64)
 
 
-__all__ = ["Oracle", "LodLevel", "adam_step", "sh", "grid_levels", "model_spec"]
+__all__ = ["Oracle", "LodLevel", "adam_step", "sh", "grid_levels", "model_spec", "mesh_frame", "voxelize"]

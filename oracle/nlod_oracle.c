@@ -676,6 +676,100 @@ int orc_first_active_voxel(const OrcLodLevel* L, const float E[3], const float D
     return 0;
 }
 
+/* ---------------------------------------------------------------------------------------------
+ * Conservative surface voxelization (restating neural_lod/cuda_voxelizer/src/voxelize.cu:58-190,
+ * the kernel the reference pipeline runs; cpu_voxelizer.cpp:39-190 is the same test) with glm
+ * 0.9.9.8's arithmetic: dot = (a.x*b.x + a.y*b.y) + a.z*b.z, cross = (a.y*b.z - b.y*a.z, ...),
+ * normalize(v) = v * (1 / sqrt(dot(v, v))), min/max/clamp by comparison.  One IEEE rounding per
+ * operation (built with -ffp-contract=off).
+ * ------------------------------------------------------------------------------------------- */
+static float orc_fmin(float a, float b) { return (b < a) ? b : a; }
+static float orc_fmax(float a, float b) { return (a < b) ? b : a; }
+static float orc_dot3(const float a[3], const float b[3]) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+static float orc_dot2(float a0, float a1, float b0, float b1) { return a0 * b0 + a1 * b1; }
+
+/* createMeshBBCube (util.h:87-112): cube around the mesh bbox, padded by epsilon * extent. */
+void orc_mesh_frame(const float mn[3], const float mx[3], uint32_t grid, float eps, float bmin[3], float bmax[3], float unit[3]) {
+    float len[3];
+    for (int i = 0; i < 3; ++i) len[i] = mx[i] - mn[i];
+    const float ml = orc_fmax(len[0], orc_fmax(len[1], len[2]));
+    for (int i = 0; i < 3; ++i) {
+        bmin[i] = mn[i];
+        bmax[i] = mx[i];
+        if (ml == len[i]) continue;
+        const float delta = ml - len[i];
+        bmin[i] = mn[i] - delta / 2.0f;
+        bmax[i] = mx[i] + delta / 2.0f;
+    }
+    if (eps != 0.f) {
+        float e[3];
+        for (int i = 0; i < 3; ++i) e[i] = (bmax[i] - bmin[i]) * eps;
+        for (int i = 0; i < 3; ++i) { bmin[i] -= e[i]; bmax[i] += e[i]; }
+    }
+    for (int i = 0; i < 3; ++i) unit[i] = (bmax[i] - bmin[i]) / (float)grid;   /* voxinfo, util.h:58-63 */
+}
+
+void orc_voxelize(const float* tris, int64_t n, const float bmin[3], const float unit[3], uint32_t grid, uint32_t* bits) {
+    const float gmax = (float)(grid - 1);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t t = 0; t < n; ++t) {
+        const float* T = tris + 9 * t;
+        float v0[3], v1[3], v2[3], e0[3], e1[3], e2[3], cr[3], nrm[3];
+        for (int i = 0; i < 3; ++i) { v0[i] = T[i] - bmin[i]; v1[i] = T[3 + i] - bmin[i]; v2[i] = T[6 + i] - bmin[i]; }
+        for (int i = 0; i < 3; ++i) { e0[i] = v1[i] - v0[i]; e1[i] = v2[i] - v1[i]; e2[i] = v0[i] - v2[i]; }
+        cr[0] = e0[1] * e1[2] - e1[1] * e0[2];
+        cr[1] = e0[2] * e1[0] - e1[2] * e0[0];
+        cr[2] = e0[0] * e1[1] - e1[0] * e0[1];
+        const float inv_len = 1.0f / sqrtf(orc_dot3(cr, cr));
+        for (int i = 0; i < 3; ++i) nrm[i] = cr[i] * inv_len;
+        int32_t lo[3], hi[3];
+        for (int i = 0; i < 3; ++i) {
+            const float wmin = orc_fmin(v0[i], orc_fmin(v1[i], v2[i])), wmax = orc_fmax(v0[i], orc_fmax(v1[i], v2[i]));
+            lo[i] = (int32_t)orc_fmin(orc_fmax(wmin / unit[i], 0.0f), gmax);
+            hi[i] = (int32_t)orc_fmin(orc_fmax(wmax / unit[i], 0.0f), gmax);
+        }
+        float c[3] = {0.f, 0.f, 0.f};
+        for (int i = 0; i < 3; ++i)
+            if (nrm[i] > 0.0f) c[i] = unit[i];
+        float cv[3], dc[3];
+        for (int i = 0; i < 3; ++i) { cv[i] = c[i] - v0[i]; dc[i] = (unit[i] - c[i]) - v0[i]; }
+        const float d1 = orc_dot3(nrm, cv), d2 = orc_dot3(nrm, dc);
+        /* edge normals in the XY, YZ and ZX planes and their offsets (axis a, axis b) */
+        const int ax[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+        const int flip_axis[3] = {2, 0, 1};
+        const float* E[3] = {e0, e1, e2};
+        const float* V[3] = {v0, v1, v2};
+        float ne[3][3][2], de[3][3];
+        for (int pl = 0; pl < 3; ++pl) {
+            const int a = ax[pl][0], b = ax[pl][1];
+            for (int k = 0; k < 3; ++k) {
+                float n0 = -1.0f * E[k][b], n1 = E[k][a];
+                if (nrm[flip_axis[pl]] < 0.0f) { n0 = -n0; n1 = -n1; }
+                ne[pl][k][0] = n0;
+                ne[pl][k][1] = n1;
+                de[pl][k] = ((-1.0f * orc_dot2(n0, n1, V[k][a], V[k][b])) + orc_fmax(0.0f, unit[a] * n0)) + orc_fmax(0.0f, unit[b] * n1);
+            }
+        }
+        for (int z = lo[2]; z <= hi[2]; ++z)
+            for (int y = lo[1]; y <= hi[1]; ++y)
+                for (int x = lo[0]; x <= hi[0]; ++x) {
+                    const float p[3] = {(float)x * unit[0], (float)y * unit[1], (float)z * unit[2]};
+                    const float nd = orc_dot3(nrm, p);
+                    if ((nd + d1) * (nd + d2) > 0.0f) continue;
+                    int ok = 1;
+                    for (int pl = 0; pl < 3 && ok; ++pl) {
+                        const int a = ax[pl][0], b = ax[pl][1];
+                        for (int k = 0; k < 3; ++k)
+                            if (orc_dot2(ne[pl][k][0], ne[pl][k][1], p[a], p[b]) + de[pl][k] < 0.0f) { ok = 0; break; }
+                    }
+                    if (!ok) continue;
+                    const uint64_t loc = (uint64_t)x + (uint64_t)y * grid + (uint64_t)z * grid * grid;
+#pragma omp atomic
+                    bits[loc >> 5] |= 1u << (31 - (loc & 31));
+                }
+    }
+}
+
 void orc_first_active_voxel_batch(const OrcLodLevel* L, int64_t n, const float* eye, const float* dir, const float* t_min,
                                   const int32_t* prev, int32_t* hit, int32_t* ijk, float* t_near, float* t_far) {
 #pragma omp parallel for schedule(dynamic, 64)

@@ -135,6 +135,15 @@ void orc_first_active_voxel_batch(const OrcLodLevel* level, int64_t n, const flo
                                   const float* t_min, const int32_t* prev, int32_t* hit, int32_t* ijk,
                                   float* t_near, float* t_far);
 
+/* createMeshBBCube + voxinfo (cuda_voxelizer/src/util.h:87-112, 58-63): cube frame around the mesh
+ * bbox, padded by eps * extent, and the voxel size (bmax - bmin) / grid per axis. */
+void orc_mesh_frame(const float mn[3], const float mx[3], uint32_t grid, float eps, float bmin[3], float bmax[3], float unit[3]);
+
+/* Conservative surface voxelization of n triangles (9 floats each) into grid^3 bits, OR-ed into
+ * `bits` (bit x + y*grid + z*grid^2, most significant bit first per word), following
+ * voxelize_triangle (cuda_voxelizer/src/voxelize.cu:58-190) in IEEE single precision. */
+void orc_voxelize(const float* tris, int64_t n, const float bmin[3], const float unit[3], uint32_t grid, uint32_t* bits);
+
 /* FP32 scalar forward over all host threads: the timed CPU baseline. Returns threads used. */
 int orc_forward_f32(const OrcModel* m, int64_t n, const float* in, const float* params, const float* max_level,
                     float max_level_scalar, float* out, int n_threads);
