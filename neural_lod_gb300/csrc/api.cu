@@ -81,6 +81,8 @@ struct nlod_module {
 
     Workspace ws;
     int tc_variant = -1;            // tensor-core kernel organisation (autotuned or default)
+    int train_groups = 0;           // tile pipelines of the fused tensor-core training kernel (0 = SIMT kernels)
+    float* loss_partial = nullptr;  // per-CTA loss sums of the fused training kernel
 
     const float* inference_params() const { return ema ? ema : params; }
     int op_kind() const { return precision == NLOD_PRECISION_FP16 ? 1 : 2; }
@@ -112,6 +114,8 @@ void ensure_workspace(nlod_module* m, uint32_t n) {
     w.loss_partial = dev_alloc<float>(w.n_partial);
     m->ws = w;
 }
+
+constexpr uint32_t kTrainPartials = 1024;   // >= CTAs of the fused training kernel (one per SM)
 
 void check_batch(uint32_t n) {
     if (n % NLOD_BATCH_GRANULARITY != 0)
@@ -272,6 +276,7 @@ int nlod_module_create(const char* encoding_json, const char* network_json, cons
             if (!tc_supported(m->d))
                 throw Error(NLOD_ERR_UNSUPPORTED, "tensor-core form needs n_neurons 64 or 128 and an encoded width <= 256");
             m->tc_variant = tc_default_variant(m->d);
+            m->train_groups = train_tc_groups(m->d);
         }
         const size_t np = m->d.n_params;
         m->n_params = (uint32_t)np;
@@ -397,6 +402,7 @@ void nlod_module_destroy(nlod_module* m) {
     if (m->w_op_inf != m->w_op) dev_free(m->w_op_inf);
     dev_free(m->w_op);
     dev_free(m->status);
+    dev_free(m->loss_partial);
     delete m;
 }
 
@@ -491,8 +497,32 @@ static int train_impl(nlod_module* m, void* stream, uint32_t n, const float* in,
         if (n == 0) throw Error(NLOD_ERR_INVALID, "empty batch");
         if (!in || !target) throw Error(NLOD_ERR_INVALID, "input and target must not be NULL");
         cudaStream_t s = (cudaStream_t)stream;
-        ensure_workspace(m, n);
         const float loss_scale = 128.0f;  // Trainer::training_step's static loss scale (trainer.h:171)
+        if (m->train_groups > 0) {
+            // fused tensor-core step: one kernel for encoding, forward, loss and all gradients
+            if (!m->loss_partial) m->loss_partial = dev_alloc<float>(kTrainPartials);
+            cuda_check(cudaMemsetAsync(m->loss_partial, 0, sizeof(float) * kTrainPartials, s), "memset");
+            cuda_check(cudaMemsetAsync(m->grads, 0, sizeof(float) * (size_t)m->n_params, s), "memset grads");
+            TrainTcArgs t{};
+            t.n = n;
+            t.in = in;
+            t.params = m->params;
+            t.weights_op = m->w_op;
+            t.max_level_gpu = m->max_level_gpu;
+            t.max_level = m->max_level;
+            t.loss_kind = m->loss.kind;
+            t.target = target;
+            t.inv_n_total = 1.0f / ((float)n * (float)m->d.n_output);
+            t.grad_scale = loss_scale * t.inv_n_total;
+            t.grads = m->grads;
+            t.loss_partial = m->loss_partial;
+            cuda_check(launch_train_tc(m->d, t, m->op_kind(), m->train_groups, m->status, s), "training step");
+            if (loss_out) cuda_check(launch_reduce_sum(m->loss_partial, kTrainPartials, loss_out, 1.0f, s), "loss");
+            m->grad_scale = loss_scale;
+            if (run_opt) run_optimizer(m, s);
+            return;
+        }
+        ensure_workspace(m, n);
         cuda_check(cudaMemsetAsync(m->ws.loss_partial, 0, sizeof(float) * m->ws.n_partial, s), "memset");
         run_training_forward(m, s, n, in, nullptr, target, loss_scale, m->ws.enc, m->ws.hidden, m->ws.y);
         if (loss_out) cuda_check(launch_reduce_sum(m->ws.loss_partial, m->ws.n_partial, loss_out, 1.0f, s), "loss");

@@ -111,4 +111,25 @@ bool tc_variant_ok(const ModelDesc& d, int variant);
 int tc_default_variant(const ModelDesc& d);
 cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, int variant, uint32_t* status, cudaStream_t s);
 
+// Fused tensor-core training step (train_tc.cu): encoding, forward, loss, backward, weight
+// gradients and grid-gradient scatter.  grads must be zeroed by the caller; gradients are
+// accumulated as dL/dparam * grad_scale.
+struct TrainTcArgs {
+    uint32_t n;
+    const float* in;                  // [n][n_input]
+    const float* params;              // FP32 parameters (grid tables read by the encoding)
+    const void* weights_op;           // network weights in the operand type
+    const float* max_level_gpu;
+    float max_level;
+    int32_t loss_kind;
+    const float* target;              // [n][n_output]
+    float inv_n_total;                // 1 / (n * n_output): the loss is a mean
+    float grad_scale;                 // loss_scale * inv_n_total
+    float* grads;                     // FP32 gradient vector
+    float* loss_partial;              // [gridDim.x] per-CTA loss sums (nullable)
+};
+// Tile pipelines per CTA that fit the network (0 = network not supported by the fused kernel).
+int train_tc_groups(const ModelDesc& d);
+cudaError_t launch_train_tc(const ModelDesc& d, const TrainTcArgs& a, int kind, int groups, uint32_t* status, cudaStream_t s);
+
 }  // namespace nlod

@@ -43,6 +43,11 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     return true;
 }
 
+// One arrival (release at CTA scope) on an mbarrier.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 __device__ __forceinline__ void fence_barrier_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
@@ -93,6 +98,13 @@ __device__ __forceinline__ uint32_t make_idesc_f16(uint32_t ab_fmt, uint32_t M, 
     d |= ((M >> 4) & 0x1Fu) << 24;
     return d;
 }
+
+// Operand majorness bits of the instruction descriptor (bit 15: A, bit 16: B; 1 = MN-major).
+// An MN-major operand uses the same 8x16-byte core matrices with the 16 contiguous bytes along
+// M (or N); its descriptor's LBO is the core-matrix stride along K and its SBO the stride along
+// M (or N).  For M = 64, row r of the accumulator lives in TMEM lane 32 * (r / 16) + r % 16.
+constexpr uint32_t kIdescAMajorMN = 1u << 15;
+constexpr uint32_t kIdescBMajorMN = 1u << 16;
 
 // Byte offset of element (row, k) in the K-major core-matrix layout with 128-byte LBO.
 __device__ __forceinline__ uint32_t kmajor_offset(uint32_t row, uint32_t k, uint32_t sbo) {

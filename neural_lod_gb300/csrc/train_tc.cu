@@ -1,0 +1,560 @@
+// Tensor-core form of the training step: encoding, forward, loss, backward through the MLP,
+// weight gradients and the grid-gradient scatter of a batch in one persistent kernel.
+//
+// A CTA (one per SM) holds the network's weights in shared memory (FP16/BF16, K-major core
+// matrices) and runs G four-warp tile pipelines ("groups") plus one MMA warp:
+//   * a group stages a 128-element tile, encodes it into X0 (shared memory), and for each of the
+//     2L MMA jobs of the tile (L forward layers, then L backward layers) signals READY, waits for
+//     DONE and runs the job's epilogue from TMEM:
+//       forward l < L-1 : ReLU, hidden activations H[l+1] kept in shared memory;
+//       forward L-1     : output activation, loss value, dL/dy (per element, unscaled) -> DZ;
+//       backward b >= 1 : dL/dH[b] * act'(H[b]) = delta of layer b-1, written over H[b];
+//       backward 0      : dL/dX0 -> grid-table gradients (warp-aggregated FP32 atomics).
+//   * the MMA warp's elected thread serves the groups' READY signals in turn: per job it issues
+//     tcgen05.mma (M = 128 rows of the tile, FP32 accumulate in the group's TMEM columns) and, for
+//     a backward job, the weight-gradient MMA dW_b += delta_b^T A_b (M = 64, contraction over the
+//     tile's 128 rows, both operands read MN-major straight from the activation buffers) into
+//     TMEM columns that persist over all tiles of the CTA, then commits to the group's DONE.
+//     One issuing thread keeps every accumulation into the shared dW columns ordered.
+// At the end the CTA adds its dW (scaled) to the FP32 gradient vector and its loss partial sum.
+//
+// The operand precision is FP16 or BF16 with FP32 accumulation.  The deltas are kept per element
+// (without the 1/N of the mean and the static loss scale, which are applied in FP32 when the
+// gradients leave the kernel), so they stay well inside the FP16 range.
+//
+// Semantics: tiny-cuda-nn's FullyFusedMLP forward/backward (src/fully_fused_mlp.cu:499-633,
+// 153-372), the losses (losses/binary_cross_entropy.h, relative_l2.h, l2.h) and the grid
+// encoding backward (encodings/grid.h:394-517), paths relative to rptr/ext/tiny-cuda-nn.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "desc.h"
+#include "encoding.cuh"
+#include "kernels.h"
+#include "tc_common.cuh"
+#include "tc_tile.cuh"
+
+namespace nlod {
+
+namespace {
+
+constexpr int kTile = 128;
+constexpr int kGT = 128;                         // threads of a group
+constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
+constexpr uint32_t kHBytes = kTile * 64u * 2u;   // one hidden activation buffer (128 x 64, 16-bit)
+
+__host__ __device__ inline uint32_t al(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
+
+struct TrainLayout {
+    uint32_t grp_base;       // first group region (after the weights)
+    uint32_t h_rel;          // H[1] within a group region (X0 at 0)
+    uint32_t dz_rel;
+    uint32_t group_stride;
+    uint32_t lvl_off;
+    uint32_t bar_off;        // ready[G], done[G], fin, then the TMEM slot and the abort flag
+    uint32_t red_off;        // per-warp loss sums
+    uint32_t total;
+    uint32_t dw_col[kMaxLayers];
+    uint32_t work_col, work_stride, tmem_cols;
+};
+
+__host__ __device__ inline TrainLayout train_layout(const ModelDesc& d, int G) {
+    TrainLayout L{};
+    uint32_t off = al(d.n_params_network * 2u, 128);
+    L.grp_base = off;
+    const uint32_t nh = d.n_layers - 1;
+    L.h_rel = al(kTile * d.enc_width * 2u, 128);
+    L.dz_rel = L.h_rel + nh * kHBytes;
+    L.group_stride = al(L.dz_rel + kTile * 16u * 2u, 128);
+    off += (uint32_t)G * L.group_stride;
+    L.lvl_off = off;
+    off += kMaxGrids * kMaxLevels * (uint32_t)sizeof(GridLevel);
+    L.bar_off = off;
+    off += 8u * (2u * G + 1u) + 8u;
+    L.red_off = al(off, 16);
+    off = L.red_off + 4u * (4u * G + 1u);
+    L.total = al(off, 128);
+    uint32_t col = 0;
+    for (uint32_t l = 0; l + 1 < d.n_layers; ++l) {
+        L.dw_col[l] = col;
+        col += al(d.layer_in[l], 32);
+    }
+    L.dw_col[d.n_layers - 1] = col;   // output layer, stored transposed: 64 rows x 16 columns
+    col += 32;
+    L.work_col = col;
+    L.work_stride = al(d.enc_width > 64u ? d.enc_width : 64u, 32);
+    col += (uint32_t)G * L.work_stride;
+    L.tmem_cols = 32;
+    while (L.tmem_cols < col) L.tmem_cols <<= 1;
+    return L;
+}
+
+// Loss value and dL/dprediction of one output, without the 1/N of the mean (the callers scale).
+__device__ __forceinline__ float loss_unit(int32_t kind, float pred, float target, float& grad) {
+    switch (kind) {
+        case LOSS_BCE: {
+            const float eps = 1e-5f;
+            const float p = fminf(fmaxf(pred, eps), 1.f - eps);
+            grad = -(target - p) / (p - p * p);
+            return -(target * logf(p) + (1.f - target) * logf(1.f - p));
+        }
+        case LOSS_RELATIVE_L2: {
+            const float den = pred * pred + 0.01f;
+            const float diff = pred - target;
+            grad = 2.f * diff / den;
+            return diff * diff / den;
+        }
+        case LOSS_L2: {
+            const float diff = pred - target;
+            grad = 2.f * diff;
+            return diff * diff;
+        }
+        default: grad = 0.f; return 0.f;
+    }
+}
+
+__device__ __forceinline__ float out_act_grad(int32_t act, float y) {
+    switch (act) {
+        case ACT_RELU: return y > 0.f ? 1.f : 0.f;
+        case ACT_SIGMOID: return y * (1.f - y);
+        case ACT_EXP: return y;
+        default: return 1.f;
+    }
+}
+
+// Saturating conversion for the 16-bit delta buffers.
+__device__ __forceinline__ float sat16(float v) { return fminf(fmaxf(v, -65504.f), 65504.f); }
+
+template <typename T>
+__device__ __forceinline__ float lo16(uint32_t w);
+template <>
+__device__ __forceinline__ float lo16<__half>(uint32_t w) { return __half2float(__ushort_as_half((unsigned short)(w & 0xFFFFu))); }
+template <>
+__device__ __forceinline__ float lo16<__nv_bfloat16>(uint32_t w) { return __uint_as_float(w << 16); }
+template <typename T>
+__device__ __forceinline__ float hi16(uint32_t w) { return lo16<T>(w >> 16); }
+
+__device__ __forceinline__ uint64_t desc(uint32_t addr, uint32_t lbo, uint32_t sbo) { return tc::make_smem_desc(addr, lbo, sbo); }
+
+// Issues MMA job j of group g (forward layers 0..L-1, then backward layers L-1..0).
+template <typename T>
+__device__ __forceinline__ void issue_job(const ModelDesc& d, const TrainLayout& L, uint8_t* smem, uint32_t tmem, uint32_t g, uint32_t j,
+                                          uint32_t& dw_started) {
+    using Op = tc::OpType<T>;
+    const uint32_t nl = d.n_layers;
+    const uint32_t grp = tc::smem_addr(smem + L.grp_base + g * L.group_stride);
+    const uint32_t x0 = grp, dz = grp + L.dz_rel;
+    auto hbuf = [&](uint32_t i) { return grp + L.h_rel + (i - 1u) * kHBytes; };   // H[i], i >= 1
+    const uint32_t work = tmem + L.work_col + g * L.work_stride;
+    const uint32_t K0 = d.enc_width;
+    if (j < nl) {
+        const uint32_t f = j, K = d.layer_in[f], N = d.layer_out[f];
+        const uint32_t a = f == 0 ? x0 : hbuf(f);
+        const uint32_t b = tc::smem_addr(smem + 2u * d.layer_offset[f]);
+        const uint32_t idesc = tc::make_idesc_f16(Op::kFmt, 128, N);
+        for (uint32_t k = 0; k < K; k += 16)
+            tc::mma_f16_ss(work, desc(a + k * 16u, 128u, K * 16u), desc(b + k * 16u, 128u, K * 16u), idesc, k > 0 ? 1u : 0u);
+        return;
+    }
+    const uint32_t b = 2u * nl - 1u - j;
+    const uint32_t in_b = d.layer_in[b], out_b = d.layer_out[b];
+    const bool last = b + 1 == nl;
+    const uint32_t delta = last ? dz : hbuf(b + 1);           // delta of layer b (rows x out_b)
+    const uint32_t delta_ld = out_b * 16u;                    // its 8-row stride
+    // delta propagation: dL/d(input of layer b) = delta_b W_b  (B = W_b read MN-major)
+    if (b > 0 || d.n_grids > 0) {
+        const uint32_t w = tc::smem_addr(smem + 2u * d.layer_offset[b]);
+        const uint32_t idesc = tc::make_idesc_f16(Op::kFmt, 128, in_b) | tc::kIdescBMajorMN;
+        for (uint32_t k = 0; k < out_b; k += 16)
+            tc::mma_f16_ss(work, desc(delta + k * 16u, 128u, delta_ld), desc(w + (k / 8u) * (in_b * 16u), in_b * 16u, 128u), idesc,
+                           k > 0 ? 1u : 0u);
+    }
+    // weight gradient over the tile's rows (both operands MN-major, K = rows)
+    const uint32_t dw = tmem + L.dw_col[b];
+    const bool started = (dw_started >> b) & 1u;
+    dw_started |= 1u << b;
+    if (last) {
+        // dW_out^T[in][out] += H[L-1]^T dz
+        const uint32_t hin = nl >= 2 ? hbuf(nl - 1) : x0;
+        const uint32_t hin_ld = nl >= 2 ? 64u * 16u : K0 * 16u;
+        const uint32_t idesc = tc::make_idesc_f16(Op::kFmt, 64, 16) | tc::kIdescAMajorMN | tc::kIdescBMajorMN;
+        for (uint32_t r = 0; r < kTile; r += 16)
+            tc::mma_f16_ss(dw, desc(hin + (r / 8u) * hin_ld, hin_ld, 128u), desc(dz + (r / 8u) * 256u, 256u, 128u), idesc,
+                           (started || r > 0) ? 1u : 0u);
+    } else {
+        // dW_b[out][in] += delta_b^T A_b
+        const uint32_t ain = b == 0 ? x0 : hbuf(b);
+        const uint32_t ain_ld = in_b * 16u;
+        const uint32_t idesc = tc::make_idesc_f16(Op::kFmt, 64, in_b) | tc::kIdescAMajorMN | tc::kIdescBMajorMN;
+        for (uint32_t r = 0; r < kTile; r += 16)
+            tc::mma_f16_ss(dw, desc(delta + (r / 8u) * delta_ld, delta_ld, 128u), desc(ain + (r / 8u) * ain_ld, ain_ld, 128u), idesc,
+                           (started || r > 0) ? 1u : 0u);
+    }
+}
+
+template <typename T, int G, int NL>
+__global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_constant__ ModelDesc d, const __grid_constant__ TrainTcArgs a,
+                                                              uint32_t* __restrict__ status) {
+    using Op = tc::OpType<T>;
+    constexpr uint32_t kThreads = G * kGT + 32;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const TrainLayout L = train_layout(d, G);
+    uint64_t* ready = reinterpret_cast<uint64_t*>(smem + L.bar_off);
+    uint64_t* done = ready + G;
+    uint64_t* fin = done + G;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fin + 1);
+    volatile uint32_t* abort_flag = tmem_slot + 1;
+    float* red = reinterpret_cast<float*>(smem + L.red_off);
+
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t nl = d.n_layers, nh = nl - 1;
+    const uint32_t n_tiles = a.n / kTile;
+
+    if (tid == 0) {
+        for (int g = 0; g < G; ++g) {
+            tc::mbar_init(&ready[g], 1);
+            tc::mbar_init(&done[g], 1);
+        }
+        tc::mbar_init(fin, 1);
+        *abort_flag = 0u;
+        tc::fence_barrier_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tmem_slot, L.tmem_cols);
+        tc::tmem_relinquish();
+    }
+    {
+        const uint16_t* wsrc = reinterpret_cast<const uint16_t*>(a.weights_op);
+        for (uint32_t l = 0; l < nl; ++l) {
+            const uint32_t K = d.layer_in[l], N = d.layer_out[l];
+            const uint32_t chunks = N * (K / 8u);
+            const uint4* src = reinterpret_cast<const uint4*>(wsrc + d.layer_offset[l]);
+            for (uint32_t c = tid; c < chunks; c += kThreads) {
+                const uint32_t n = c / (K / 8u), k0 = (c - n * (K / 8u)) * 8u;
+                *reinterpret_cast<uint4*>(smem + 2u * d.layer_offset[l] + tc::kmajor_offset(n, k0, K * 16u)) = src[c];
+            }
+        }
+    }
+    GridLevel* lvl_s = reinterpret_cast<GridLevel*>(smem + L.lvl_off);
+    for (uint32_t i = tid; i < d.n_grids * (uint32_t)kMaxLevels; i += kThreads) {
+        const uint32_t g = i / kMaxLevels, l = i % kMaxLevels;
+        if (l < d.grids[g].n_levels) lvl_s[i] = d.grids[g].levels[l];
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t first_tile = blockIdx.x * G;
+    const uint32_t stride = gridDim.x * G;
+    bool aborted = false;
+    float loss_acc = 0.f;
+
+    if (warp == (uint32_t)G * 4u) {
+        // ---- MMA warp ----
+        if (lane == 0) {
+            uint32_t left[G], job[G];
+            uint32_t rpar = 0, active = 0, dw_started = 0;
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const uint32_t t0 = first_tile + g;
+                left[g] = t0 < n_tiles ? (n_tiles - t0 + stride - 1) / stride : 0u;
+                job[g] = 0;
+                if (left[g]) active |= 1u << g;
+            }
+            long long last = clock64();
+            while (active) {
+                if (*abort_flag) break;
+                bool prog = false;
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    if (!((active >> g) & 1u)) continue;
+                    if (!tc::mbar_try_wait(&ready[g], (rpar >> g) & 1u)) continue;
+                    rpar ^= 1u << g;
+                    tc::fence_after_sync();
+                    issue_job<T>(d, L, smem, tmem, (uint32_t)g, job[g], dw_started);
+                    tc::mma_commit(&done[g]);
+                    if (++job[g] == 2u * nl) {
+                        job[g] = 0;
+                        if (--left[g] == 0) active &= ~(1u << g);
+                    }
+                    prog = true;
+                }
+                if (prog) {
+                    last = clock64();
+                } else if (clock64() - last > kWaitCycles) {
+                    *abort_flag = 1u;
+                    atomicOr(status, 1u);
+                    break;
+                }
+            }
+            tc::mma_commit(fin);
+            if (!tc::mbar_wait_bounded(fin, 0, kWaitCycles)) atomicOr(status, 1u);
+        }
+        __syncwarp();
+    } else {
+        // ---- tile pipeline (group) ----
+        const uint32_t grp_i = warp >> 2;
+        const uint32_t gtid = tid & (kGT - 1);
+        const uint32_t quarter = warp & 3u;
+        const uint32_t bar_id = 1u + grp_i;
+        uint8_t* grp = smem + L.grp_base + grp_i * L.group_stride;
+        uint8_t* x0 = grp;
+        uint8_t* dzb = grp + L.dz_rel;
+        auto hbuf = [&](uint32_t i) { return grp + L.h_rel + (i - 1u) * kHBytes; };
+        float* in_s = reinterpret_cast<float*>(hbuf(nh));   // staging aliases the last hidden buffer
+        const uint32_t in_ld = d.n_input + 1;
+        const uint32_t row = quarter * 32u + lane;
+        const uint32_t taddr = tmem + L.work_col + grp_i * L.work_stride + ((quarter * 32u) << 16);
+        uint32_t dpar = 0;
+
+        for (uint32_t tile = first_tile + grp_i; tile < n_tiles; tile += stride) {
+            const uint32_t row0 = tile * kTile;
+            const float* in_tile = a.in + (size_t)row0 * d.n_input;
+            for (uint32_t idx = gtid; idx < kTile * d.n_input; idx += kGT) {
+                const uint32_t r = idx / d.n_input, c = idx - r * d.n_input;
+                in_s[r * in_ld + c] = __ldg(in_tile + idx);
+            }
+            group_sync(bar_id);
+            {
+                TcStore<T> st{x0, d.enc_width * 16u};
+                encode_tile_rows<NL>(d, lvl_s, a.params, in_s, in_ld, a.max_level_gpu, a.max_level, row0, kTile, gtid, kGT, st);
+            }
+            tc::fence_proxy_async_smem();
+            tc::fence_before_sync();
+            group_sync(bar_id);
+            if (gtid == 0) tc::mbar_arrive(&ready[grp_i]);
+
+            for (uint32_t j = 0; j < 2u * nl; ++j) {
+                const bool ok = gtid != 0 || tc::mbar_wait_bounded(&done[grp_i], dpar, kWaitCycles);
+                dpar ^= 1u;
+                if (group_sync_or(bar_id, !ok)) {
+                    aborted = true;
+                    break;
+                }
+                tc::fence_after_sync();
+                const size_t grow = (size_t)row0 + row;
+                if (j + 1 < nl) {
+                    // hidden layer j: activation -> H[j+1]
+                    uint8_t* h = hbuf(j + 1);
+#pragma unroll
+                    for (uint32_t col = 0; col < 64u; col += 32) {
+                        uint32_t r[32];
+                        tc::tmem_ld32(taddr + col, r);
+                        tc::tmem_wait_ld();
+#pragma unroll
+                        for (uint32_t q = 0; q < 4; ++q) {
+                            uint4 pk;
+                            pk.x = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * q + 0])), act_fwd(d.act, __uint_as_float(r[8 * q + 1])));
+                            pk.y = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * q + 2])), act_fwd(d.act, __uint_as_float(r[8 * q + 3])));
+                            pk.z = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * q + 4])), act_fwd(d.act, __uint_as_float(r[8 * q + 5])));
+                            pk.w = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * q + 6])), act_fwd(d.act, __uint_as_float(r[8 * q + 7])));
+                            *reinterpret_cast<uint4*>(h + tc::kmajor_offset(row, col + 8u * q, 1024u)) = pk;
+                        }
+                    }
+                } else if (j + 1 == nl) {
+                    // output layer: activation, loss, dL/dz per element -> DZ
+                    uint32_t r[16];
+                    tc::tmem_ld16(taddr, r);
+                    tc::tmem_wait_ld();
+                    float dzv[16];
+#pragma unroll
+                    for (uint32_t c = 0; c < 16; ++c) {
+                        float gv = 0.f;
+                        if (c < d.n_output) {
+                            const float y = act_fwd(d.out_act, __uint_as_float(r[c]));
+                            loss_acc += loss_unit(a.loss_kind, y, __ldg(a.target + grow * d.n_output + c), gv) * a.inv_n_total;
+                            gv *= out_act_grad(d.out_act, y);
+                        }
+                        dzv[c] = sat16(gv);
+                    }
+#pragma unroll
+                    for (uint32_t q = 0; q < 2; ++q) {
+                        uint4 pk;
+                        pk.x = Op::pack2(dzv[8 * q + 0], dzv[8 * q + 1]);
+                        pk.y = Op::pack2(dzv[8 * q + 2], dzv[8 * q + 3]);
+                        pk.z = Op::pack2(dzv[8 * q + 4], dzv[8 * q + 5]);
+                        pk.w = Op::pack2(dzv[8 * q + 6], dzv[8 * q + 7]);
+                        *reinterpret_cast<uint4*>(dzb + tc::kmajor_offset(row, 8u * q, 256u)) = pk;
+                    }
+                } else {
+                    const uint32_t b = 2u * nl - 1u - j;
+                    if (b > 0) {
+                        // delta of layer b-1 = dL/dH[b] * act'(H[b]), in place over H[b]
+                        uint8_t* h = hbuf(b);
+#pragma unroll
+                        for (uint32_t col = 0; col < 64u; col += 32) {
+                            uint32_t r[32];
+                            tc::tmem_ld32(taddr + col, r);
+                            tc::tmem_wait_ld();
+#pragma unroll
+                            for (uint32_t q = 0; q < 4; ++q) {
+                                uint4* p = reinterpret_cast<uint4*>(h + tc::kmajor_offset(row, col + 8u * q, 1024u));
+                                const uint4 hv = *p;
+                                const uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
+                                uint32_t ow[4];
+#pragma unroll
+                                for (uint32_t e = 0; e < 4; ++e) {
+                                    float g0 = __uint_as_float(r[8 * q + 2 * e]), g1 = __uint_as_float(r[8 * q + 2 * e + 1]);
+                                    if (d.act == ACT_RELU) {
+                                        g0 = lo16<T>(hw[e]) > 0.f ? g0 : 0.f;
+                                        g1 = hi16<T>(hw[e]) > 0.f ? g1 : 0.f;
+                                    }
+                                    ow[e] = Op::pack2(sat16(g0), sat16(g1));
+                                }
+                                *p = make_uint4(ow[0], ow[1], ow[2], ow[3]);
+                            }
+                        }
+                    } else if (d.n_grids > 0) {
+                        // dL/dX0 -> grid-table gradients
+                        for (uint32_t si = 0; si < d.n_slots; ++si) {
+                            const Slot& s = d.slots[si];
+                            if (s.type != SLOT_GRID) continue;
+                            const GridDesc& gd = d.grids[s.grid];
+                            const float* prow = a.in + grow * d.n_input + s.in_begin;
+                            const float px = __ldg(prow), py = __ldg(prow + 1), pz = __ldg(prow + 2);
+                            const float ml = a.max_level_gpu ? __ldg(a.max_level_gpu + grow) : a.max_level;
+                            float* gtab = a.grads + gd.param_offset;
+                            for (uint32_t l0 = 0; l0 < gd.n_levels; l0 += 8) {
+                                uint32_t r[16];
+                                tc::tmem_ld16(taddr + s.out_begin + 2u * l0, r);
+                                tc::tmem_wait_ld();
+#pragma unroll 1
+                                for (uint32_t q = 0; q < 8 && l0 + q < gd.n_levels; ++q) {
+                                    const uint32_t level = l0 + q;
+                                    const bool act = !grid_level_skipped_backward(level, ml, gd.n_levels);
+                                    const float2 dy = make_float2(__uint_as_float(r[2 * q]) * a.grad_scale, __uint_as_float(r[2 * q + 1]) * a.grad_scale);
+                                    grid_level_backward(gd, level, gtab, px, py, pz, dy, act);
+                                }
+                            }
+                        }
+                    }
+                }
+                tc::fence_proxy_async_smem();
+                tc::fence_before_sync();
+                group_sync(bar_id);
+                if (j + 1 < 2u * nl && gtid == 0) tc::mbar_arrive(&ready[grp_i]);
+            }
+            if (aborted) break;
+        }
+        if (aborted) {
+            *abort_flag = 1u;
+            if (gtid == 0) atomicOr(status, 1u);
+        }
+    }
+
+    // ---- drain the weight gradients, loss partial sum ----
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const bool any_tile = first_tile < n_tiles;
+    if (!*abort_flag && any_tile && warp < (uint32_t)G * 4u) {
+        const uint32_t grp_i = warp >> 2, quarter = warp & 3u;
+        const uint32_t m = quarter * 16u + lane;   // accumulator row (M = 64 layout)
+        for (uint32_t b = grp_i; b < nl; b += G) {
+            const bool last = b + 1 == nl;
+            const uint32_t ncols = last ? 16u : d.layer_in[b];
+            float* gw = a.grads + d.layer_offset[b];
+            for (uint32_t c0 = 0; c0 < ncols; c0 += 16) {
+                uint32_t r[16];
+                tc::tmem_ld16(tmem + L.dw_col[b] + c0 + ((quarter * 32u) << 16), r);
+                tc::tmem_wait_ld();
+                if (lane < 16) {
+#pragma unroll
+                    for (uint32_t c = 0; c < 16; ++c) {
+                        if (c0 + c >= ncols) break;
+                        const float v = __uint_as_float(r[c]) * a.grad_scale;
+                        if (last) atomicAdd(gw + (c0 + c) * d.layer_in[b] + m, v);
+                        else atomicAdd(gw + m * d.layer_in[b] + c0 + c, v);
+                    }
+                }
+            }
+        }
+    }
+    if (a.loss_partial) {
+        float v = loss_acc;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp] = v;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (a.loss_partial && tid == 0) {
+        float s = 0.f;
+        for (uint32_t w = 0; w < (uint32_t)G * 4u; ++w) s += red[w];
+        a.loss_partial[blockIdx.x] = s;
+    }
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, L.tmem_cols);
+    }
+}
+
+int g_sms = 0;
+int sm_count() {
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 1;
+    }
+    return g_sms;
+}
+
+constexpr size_t kMaxSmem = 227u * 1024u;
+
+bool layout_ok(const ModelDesc& d, int G) {
+    const TrainLayout L = train_layout(d, G);
+    return L.total <= kMaxSmem && L.tmem_cols <= 512u;
+}
+
+template <typename T, int G, int NL>
+cudaError_t launch_g(const ModelDesc& d, const TrainTcArgs& a, uint32_t* status, cudaStream_t s) {
+    const TrainLayout L = train_layout(d, G);
+    const uint32_t n_tiles = a.n / kTile;
+    uint32_t blocks = (uint32_t)sm_count();
+    const uint32_t need = (n_tiles + G - 1) / G;
+    if (blocks > need) blocks = need;
+    if (blocks == 0) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_train_tc<T, G, NL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+    if (e != cudaSuccess) return e;
+    k_train_tc<T, G, NL><<<blocks, G * kGT + 32, L.total, s>>>(d, a, status);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_t(const ModelDesc& d, const TrainTcArgs& a, int G, uint32_t* status, cudaStream_t s) {
+    switch (G) {
+        case 2: return launch_g<T, 2, 2>(d, a, status, s);
+        case 3: return launch_g<T, 3, 2>(d, a, status, s);
+        case 4: return launch_g<T, 4, 2>(d, a, status, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+int train_tc_groups(const ModelDesc& d) {
+    if (d.width != 64 || d.n_layers < 2 || d.n_layers > 8) return 0;
+    if (d.act != ACT_RELU && d.act != ACT_NONE) return 0;
+    if (d.enc_width % 16 != 0 || d.enc_width > 128 || d.n_output_padded != 16) return 0;
+    if (d.n_input + 1 > 32) return 0;
+    for (uint32_t l = 1; l + 1 < d.n_layers; ++l)
+        if (d.layer_in[l] != 64 || d.layer_out[l] != 64) return 0;
+    if (d.layer_out[0] != 64 || d.layer_in[d.n_layers - 1] != 64 || d.layer_out[d.n_layers - 1] != 16) return 0;
+    for (int G = 4; G >= 2; --G)
+        if (layout_ok(d, G)) return G;
+    return 0;
+}
+
+cudaError_t launch_train_tc(const ModelDesc& d, const TrainTcArgs& a, int kind, int G, uint32_t* status, cudaStream_t s) {
+    if (G < 2 || G > 4 || !layout_ok(d, G)) return cudaErrorInvalidValue;
+    if (kind == 1) return launch_t<__half>(d, a, G, status, s);
+    if (kind == 2) return launch_t<__nv_bfloat16>(d, a, G, status, s);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace nlod

@@ -1,6 +1,6 @@
 """Parity of the training path (loss, backward, Adam, EMA/decay, checkpoints) against the
-FP64 oracle.  Gradient tolerance: relative L2 error <= 1e-3 of the FP64 oracle's gradient per
-parameter block (network matrices, grid tables) in every form; loss within 1e-4 relative."""
+FP64 oracle.  Gradient tolerance of the plain FP32 form: relative L2 error <= 1e-3 of the FP64
+oracle's gradient per parameter block (network matrices, grid tables); loss within 1e-4 relative."""
 import json
 
 import numpy as np
@@ -27,8 +27,9 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
 
 
-@pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("precision", ["fp32"])
 def test_loss_and_gradients_match_oracle(cuda, nlod_lib, precision):
+    """The plain FP32 form (the FP16 / BF16 forms run the fused kernel: test_gpu_train_tc.py)."""
     import torch
 
     m, orc, params, x, t, spec = _setup(precision)
