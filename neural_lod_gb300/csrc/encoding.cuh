@@ -233,6 +233,74 @@ __device__ __forceinline__ void grid_level_backward(const GridDesc& g, uint32_t 
     }
 }
 
+// Scatter of one linear / smoothstep-interpolated level for one element with the 8 corner
+// entries formed at once, so that the 8 atomics (and, with AGG, the 8 warp matches) are
+// independent.  AGG merges the lanes of a warp that hit the same entry before the atomic (pays
+// when a warp's elements are spatially coherent); without it every corner is one FP32x2 atomic,
+// as in tiny-cuda-nn's kernel_grid_backward.  Must be called by all lanes of the warp.
+template <bool AGG>
+__device__ __forceinline__ void grid_level_scatter8(const GridDesc& g, const GridLevel& L, float* __restrict__ grad_table, uint32_t p0,
+                                                    uint32_t p1, uint32_t p2, float px, float py, float pz, float2 dy, bool active) {
+    float2* lv = reinterpret_cast<float2*>(grad_table) + L.offset;
+    float fx, fy, fz;
+    uint32_t cx, cy, cz;
+    grid_pos_fract(px, L.scale, fx, cx);
+    grid_pos_fract(py, L.scale, fy, cy);
+    grid_pos_fract(pz, L.scale, fz, cz);
+    fx = interp_weight_fun(g.interp, fx);
+    fy = interp_weight_fun(g.interp, fy);
+    fz = interp_weight_fun(g.interp, fz);
+    uint32_t e[8];
+    level_corner_entries(L, p0, p1, p2, cx, cy, cz, e);
+    const float wx[2] = {1.0f - fx, fx};
+    const float wy[2] = {1.0f - fy, fy};
+    const float wz[2] = {1.0f - fz, fz};
+    float2 v[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const float w = wx[c & 1] * wy[(c >> 1) & 1] * wz[(c >> 2) & 1];
+        v[c] = make_float2(w * dy.x, w * dy.y);
+    }
+    if (!AGG) {
+        if (active) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) atomicAdd(lv + e[c], v[c]);
+        }
+        return;
+    }
+    const unsigned full = __activemask();
+    unsigned peers[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) peers[c] = __match_any_sync(full, active ? e[c] : 0xFFFFFFFFu);
+    bool dup = false;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) dup |= (peers[c] & (peers[c] - 1u)) != 0u;
+    if (!__any_sync(full, dup)) {
+        if (active) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) atomicAdd(lv + e[c], v[c]);
+        }
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        float2 s = v[c];
+        if (__popc(peers[c]) > 1) {
+            float sx = 0.f, sy = 0.f;
+            unsigned m = peers[c];
+            while (m) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                sx += __shfl_sync(peers[c], v[c].x, src);
+                sy += __shfl_sync(peers[c], v[c].y, src);
+            }
+            s = make_float2(sx, sy);
+        }
+        if (active && lane == __ffs(peers[c]) - 1) atomicAdd(lv + e[c], s);
+    }
+}
+
 // ---- spherical harmonics -------------------------------------------------------------------
 
 #include "sh_basis.inc"

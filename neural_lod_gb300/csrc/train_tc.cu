@@ -45,6 +45,7 @@ constexpr int kTile = 128;
 constexpr int kGT = 128;                         // threads of a group
 constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 constexpr uint32_t kHBytes = kTile * 64u * 2u;   // one hidden activation buffer (128 x 64, 16-bit)
+constexpr bool kScatterAggregate = false;        // one atomic per corner (see grid_level_scatter8)
 
 __host__ __device__ inline uint32_t al(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
 
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
 #pragma unroll
                 for (int g = 0; g < G; ++g) {
                     if (!((active >> g) & 1u)) continue;
-                    if (!tc::mbar_try_wait(&ready[g], (rpar >> g) & 1u)) continue;
+                    if (!tc::mbar_test_wait(&ready[g], (rpar >> g) & 1u)) continue;
                     rpar ^= 1u << g;
                     tc::fence_after_sync();
                     issue_job<T>(d, L, smem, tmem, (uint32_t)g, job[g], dw_started);
@@ -414,10 +415,13 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
                             const Slot& s = d.slots[si];
                             if (s.type != SLOT_GRID) continue;
                             const GridDesc& gd = d.grids[s.grid];
+                            const GridLevel* lv = lvl_s + s.grid * kMaxLevels;
                             const float* prow = a.in + grow * d.n_input + s.in_begin;
                             const float px = __ldg(prow), py = __ldg(prow + 1), pz = __ldg(prow + 2);
                             const float ml = a.max_level_gpu ? __ldg(a.max_level_gpu + grow) : a.max_level;
                             float* gtab = a.grads + gd.param_offset;
+                            uint32_t p0, p1, p2;
+                            hash_primes(gd.hash, p0, p1, p2);
                             for (uint32_t l0 = 0; l0 < gd.n_levels; l0 += 8) {
                                 uint32_t r[16];
                                 tc::tmem_ld16(taddr + s.out_begin + 2u * l0, r);
@@ -427,7 +431,8 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
                                     const uint32_t level = l0 + q;
                                     const bool act = !grid_level_skipped_backward(level, ml, gd.n_levels);
                                     const float2 dy = make_float2(__uint_as_float(r[2 * q]) * a.grad_scale, __uint_as_float(r[2 * q + 1]) * a.grad_scale);
-                                    grid_level_backward(gd, level, gtab, px, py, pz, dy, act);
+                                    if (gd.interp == INTERP_NEAREST) grid_level_backward(gd, level, gtab, px, py, pz, dy, act);
+                                    else grid_level_scatter8<kScatterAggregate>(gd, lv[level], gtab, p0, p1, p2, px, py, pz, dy, act);
                                 }
                             }
                         }
