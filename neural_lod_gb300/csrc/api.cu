@@ -83,6 +83,8 @@ struct nlod_module {
     int tc_variant = -1;            // tensor-core kernel organisation (autotuned or default)
     int train_groups = 0;           // tile pipelines of the fused tensor-core training kernel (0 = SIMT kernels)
     float* loss_partial = nullptr;  // per-CTA loss sums of the fused training kernel
+    void* enc_tiles = nullptr;      // encoded X0 tiles of the fused training step (operand type)
+    size_t enc_tiles_bytes = 0;
 
     const float* inference_params() const { return ema ? ema : params; }
     int op_kind() const { return precision == NLOD_PRECISION_FP16 ? 1 : 2; }
@@ -403,6 +405,7 @@ void nlod_module_destroy(nlod_module* m) {
     dev_free(m->w_op);
     dev_free(m->status);
     dev_free(m->loss_partial);
+    dev_free(m->enc_tiles);
     delete m;
 }
 
@@ -516,6 +519,16 @@ static int train_impl(nlod_module* m, void* stream, uint32_t n, const float* in,
             t.grad_scale = loss_scale * t.inv_n_total;
             t.grads = m->grads;
             t.loss_partial = m->loss_partial;
+            const size_t enc_bytes = (size_t)n * m->d.enc_width * 2u;
+            if (m->enc_tiles_bytes < enc_bytes) {
+                dev_free(m->enc_tiles);
+                m->enc_tiles = nullptr;
+                m->enc_tiles_bytes = 0;
+                m->enc_tiles = dev_alloc<uint8_t>(enc_bytes);
+                m->enc_tiles_bytes = enc_bytes;
+            }
+            t.enc_tiles = m->enc_tiles;
+            cuda_check(launch_encode_tiles(m->d, t, m->op_kind(), s), "encoding");
             cuda_check(launch_train_tc(m->d, t, m->op_kind(), m->train_groups, m->status, s), "training step");
             if (loss_out) cuda_check(launch_reduce_sum(m->loss_partial, kTrainPartials, loss_out, 1.0f, s), "loss");
             m->grad_scale = loss_scale;

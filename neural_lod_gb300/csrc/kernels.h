@@ -127,9 +127,13 @@ struct TrainTcArgs {
     float grad_scale;                 // loss_scale * inv_n_total
     float* grads;                     // FP32 gradient vector
     float* loss_partial;              // [gridDim.x] per-CTA loss sums (nullable)
+    void* enc_tiles;                  // [n/128][128 x enc_width] operand-type X0 tiles written by
+                                      // launch_encode_tiles; nullable (the fused kernel then encodes)
 };
 // Tile pipelines per CTA that fit the network (0 = network not supported by the fused kernel).
 int train_tc_groups(const ModelDesc& d);
 cudaError_t launch_train_tc(const ModelDesc& d, const TrainTcArgs& a, int kind, int groups, uint32_t* status, cudaStream_t s);
+// Encodes the batch into a.enc_tiles (kind 1 = FP16, 2 = BF16).
+cudaError_t launch_encode_tiles(const ModelDesc& d, const TrainTcArgs& a, int kind, cudaStream_t s);
 
 }  // namespace nlod

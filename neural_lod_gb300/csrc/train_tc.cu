@@ -55,7 +55,7 @@ struct TrainLayout {
     uint32_t dz_rel;
     uint32_t group_stride;
     uint32_t lvl_off;
-    uint32_t bar_off;        // ready[G], done[G], fin, then the TMEM slot and the abort flag
+    uint32_t bar_off;        // ready[G], done[G], fin, xbar[G], then the TMEM slot and the abort flag
     uint32_t red_off;        // per-warp loss sums
     uint32_t total;
     uint32_t dw_col[kMaxLayers];
@@ -74,7 +74,7 @@ __host__ __device__ inline TrainLayout train_layout(const ModelDesc& d, int G) {
     L.lvl_off = off;
     off += kMaxGrids * kMaxLevels * (uint32_t)sizeof(GridLevel);
     L.bar_off = off;
-    off += 8u * (2u * G + 1u) + 8u;
+    off += 8u * (3u * G + 1u) + 8u;
     L.red_off = al(off, 16);
     off = L.red_off + 4u * (4u * G + 1u);
     L.total = al(off, 128);
@@ -206,7 +206,8 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
     uint64_t* ready = reinterpret_cast<uint64_t*>(smem + L.bar_off);
     uint64_t* done = ready + G;
     uint64_t* fin = done + G;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fin + 1);
+    uint64_t* xbar = fin + 1;                    // X0 tile arrival (pre-encoded tiles)
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(xbar + G);
     volatile uint32_t* abort_flag = tmem_slot + 1;
     float* red = reinterpret_cast<float*>(smem + L.red_off);
 
@@ -218,6 +219,7 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
         for (int g = 0; g < G; ++g) {
             tc::mbar_init(&ready[g], 1);
             tc::mbar_init(&done[g], 1);
+            tc::mbar_init(&xbar[g], 1);
         }
         tc::mbar_init(fin, 1);
         *abort_flag = 0u;
@@ -310,23 +312,41 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
         const uint32_t in_ld = d.n_input + 1;
         const uint32_t row = quarter * 32u + lane;
         const uint32_t taddr = tmem + L.work_col + grp_i * L.work_stride + ((quarter * 32u) << 16);
-        uint32_t dpar = 0;
+        uint32_t dpar = 0, xpar = 0;
+        bool x_pending = false;   // a bulk copy of X0 is in flight (thread gtid 0)
+        const uint32_t x0_bytes = kTile * d.enc_width * 2u;
+        const uint8_t* enc_tiles = reinterpret_cast<const uint8_t*>(a.enc_tiles);
+        if (enc_tiles && gtid == 0 && first_tile + grp_i < n_tiles) {
+            tc::mbar_arrive_expect_tx(&xbar[grp_i], x0_bytes);
+            tc::bulk_copy_g2s(x0, enc_tiles + (size_t)(first_tile + grp_i) * x0_bytes, x0_bytes, &xbar[grp_i]);
+            x_pending = true;
+        }
 
         for (uint32_t tile = first_tile + grp_i; tile < n_tiles; tile += stride) {
             const uint32_t row0 = tile * kTile;
-            const float* in_tile = a.in + (size_t)row0 * d.n_input;
-            for (uint32_t idx = gtid; idx < kTile * d.n_input; idx += kGT) {
-                const uint32_t r = idx / d.n_input, c = idx - r * d.n_input;
-                in_s[r * in_ld + c] = __ldg(in_tile + idx);
-            }
-            group_sync(bar_id);
-            {
+            if (enc_tiles) {
+                // X0 was encoded by k_encode_tiles; its copy was issued when the previous tile's
+                // last MMA job had finished reading X0.
+                const bool ok = gtid != 0 || tc::mbar_wait_bounded(&xbar[grp_i], xpar, kWaitCycles);
+                x_pending = x_pending && !ok;
+                xpar ^= ok ? 1u : 0u;
+                if (group_sync_or(bar_id, !ok)) {
+                    aborted = true;
+                    break;
+                }
+            } else {
+                const float* in_tile = a.in + (size_t)row0 * d.n_input;
+                for (uint32_t idx = gtid; idx < kTile * d.n_input; idx += kGT) {
+                    const uint32_t r = idx / d.n_input, c = idx - r * d.n_input;
+                    in_s[r * in_ld + c] = __ldg(in_tile + idx);
+                }
+                group_sync(bar_id);
                 TcStore<T> st{x0, d.enc_width * 16u};
                 encode_tile_rows<NL>(d, lvl_s, a.params, in_s, in_ld, a.max_level_gpu, a.max_level, row0, kTile, gtid, kGT, st);
+                tc::fence_proxy_async_smem();
+                tc::fence_before_sync();
+                group_sync(bar_id);
             }
-            tc::fence_proxy_async_smem();
-            tc::fence_before_sync();
-            group_sync(bar_id);
             if (gtid == 0) tc::mbar_arrive(&ready[grp_i]);
 
             for (uint32_t j = 0; j < 2u * nl; ++j) {
@@ -383,6 +403,12 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
                     }
                 } else {
                     const uint32_t b = 2u * nl - 1u - j;
+                    if (b == 0 && enc_tiles && gtid == 0 && tile + stride < n_tiles) {
+                        // every MMA reading X0 has completed: fetch the next tile during this epilogue
+                        tc::mbar_arrive_expect_tx(&xbar[grp_i], x0_bytes);
+                        tc::bulk_copy_g2s(x0, enc_tiles + (size_t)(tile + stride) * x0_bytes, x0_bytes, &xbar[grp_i]);
+                        x_pending = true;
+                    }
                     if (b > 0) {
                         // delta of layer b-1 = dL/dH[b] * act'(H[b]), in place over H[b]
                         uint8_t* h = hbuf(b);
@@ -449,6 +475,8 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
             *abort_flag = 1u;
             if (gtid == 0) atomicOr(status, 1u);
         }
+        // a copy still in flight (only after an abort) must land before the CTA's shared memory goes
+        if (x_pending) (void)tc::mbar_wait_bounded(&xbar[grp_i], xpar, kWaitCycles);
     }
 
     // ---- drain the weight gradients, loss partial sum ----
@@ -495,6 +523,36 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
     if (warp == 0) {
         tc::fence_after_sync();
         tc::tmem_dealloc(tmem, L.tmem_cols);
+    }
+}
+
+// Encoding of the batch into X0 tiles in HBM, each tile laid out exactly as the fused kernel's
+// shared-memory A operand (128 rows x enc_width, K-major core matrices), so that one bulk copy
+// brings it in.  Full occupancy (128-thread CTAs) for the gather-bound grid levels.
+template <typename T, int NL>
+__global__ void __launch_bounds__(kTile) k_encode_tiles(const __grid_constant__ ModelDesc d, const __grid_constant__ TrainTcArgs a) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    GridLevel* lvl_s = reinterpret_cast<GridLevel*>(smem);
+    float* in_s = reinterpret_cast<float*>(smem + kMaxGrids * kMaxLevels * sizeof(GridLevel));
+    const uint32_t tid = threadIdx.x;
+    const uint32_t in_ld = d.n_input + 1;
+    for (uint32_t i = tid; i < d.n_grids * (uint32_t)kMaxLevels; i += kTile) {
+        const uint32_t g = i / kMaxLevels, l = i % kMaxLevels;
+        if (l < d.grids[g].n_levels) lvl_s[i] = d.grids[g].levels[l];
+    }
+    const uint32_t n_tiles = a.n / kTile;
+    const size_t x0_bytes = (size_t)kTile * d.enc_width * 2u;
+    for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const uint32_t row0 = tile * kTile;
+        __syncthreads();
+        const float* in_tile = a.in + (size_t)row0 * d.n_input;
+        for (uint32_t idx = tid; idx < kTile * d.n_input; idx += kTile) {
+            const uint32_t r = idx / d.n_input, c = idx - r * d.n_input;
+            in_s[r * in_ld + c] = __ldg(in_tile + idx);
+        }
+        __syncthreads();
+        TcStore<T> st{reinterpret_cast<uint8_t*>(a.enc_tiles) + tile * x0_bytes, d.enc_width * 16u};
+        encode_tile_rows<NL>(d, lvl_s, a.params, in_s, in_ld, a.max_level_gpu, a.max_level, row0, kTile, tid, kTile, st);
     }
 }
 
@@ -553,6 +611,18 @@ int train_tc_groups(const ModelDesc& d) {
     for (int G = 4; G >= 2; --G)
         if (layout_ok(d, G)) return G;
     return 0;
+}
+
+cudaError_t launch_encode_tiles(const ModelDesc& d, const TrainTcArgs& a, int kind, cudaStream_t s) {
+    const uint32_t n_tiles = a.n / kTile;
+    if (n_tiles == 0) return cudaSuccess;
+    uint32_t blocks = (uint32_t)sm_count() * 16u;
+    if (blocks > n_tiles) blocks = n_tiles;
+    const size_t smem = kMaxGrids * kMaxLevels * sizeof(GridLevel) + (size_t)kTile * (d.n_input + 1) * 4u;
+    if (kind == 1) k_encode_tiles<__half, 2><<<blocks, kTile, smem, s>>>(d, a);
+    else if (kind == 2) k_encode_tiles<__nv_bfloat16, 2><<<blocks, kTile, smem, s>>>(d, a);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
 }
 
 cudaError_t launch_train_tc(const ModelDesc& d, const TrainTcArgs& a, int kind, int G, uint32_t* status, cudaStream_t s) {
