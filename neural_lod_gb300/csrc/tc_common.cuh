@@ -57,7 +57,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     return true;
 }
 
-// One arrival (release at CTA scope) on an mbarrier.
 // One arrival that also announces `bytes` of asynchronous transfers the phase must wait for.
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
@@ -70,6 +69,7 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
                  : "memory");
 }
 
+// One arrival (release at CTA scope) on an mbarrier.
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
@@ -154,6 +154,11 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 }
 
 // ---- TMEM -> registers ----------------------------------------------------------------------
+
+// 32 lanes x 32 bits, 2 consecutive columns per thread.
+__device__ __forceinline__ void tmem_ld2(uint32_t taddr, uint32_t& r0, uint32_t& r1) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r0), "=r"(r1) : "r"(taddr));
+}
 
 // 32 lanes x 32 bits, 16 consecutive columns per thread.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {

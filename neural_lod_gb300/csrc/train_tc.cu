@@ -58,9 +58,16 @@ struct TrainLayout {
     uint32_t bar_off;        // ready[G], done[G], fin, xbar[G], then the TMEM slot and the abort flag
     uint32_t red_off;        // per-warp loss sums
     uint32_t total;
-    uint32_t dw_col[kMaxLayers];
-    uint32_t work_col, work_stride, tmem_cols;
+    uint32_t work_col, work_stride, tmem_cols;   // TMEM: dW columns of every layer, then G work regions
 };
+
+// First TMEM column of layer b's weight-gradient accumulator (layers in order, each rounded up to
+// 32 columns; the output layer's is stored transposed, 64 rows x 16 columns).
+__host__ __device__ inline uint32_t dw_col(const ModelDesc& d, uint32_t b) {
+    uint32_t col = 0;
+    for (uint32_t l = 0; l < b; ++l) col += (l + 1 < d.n_layers) ? al(d.layer_in[l], 32) : 32u;
+    return col;
+}
 
 __host__ __device__ inline TrainLayout train_layout(const ModelDesc& d, int G) {
     TrainLayout L{};
@@ -78,13 +85,7 @@ __host__ __device__ inline TrainLayout train_layout(const ModelDesc& d, int G) {
     L.red_off = al(off, 16);
     off = L.red_off + 4u * (4u * G + 1u);
     L.total = al(off, 128);
-    uint32_t col = 0;
-    for (uint32_t l = 0; l + 1 < d.n_layers; ++l) {
-        L.dw_col[l] = col;
-        col += al(d.layer_in[l], 32);
-    }
-    L.dw_col[d.n_layers - 1] = col;   // output layer, stored transposed: 64 rows x 16 columns
-    col += 32;
+    uint32_t col = dw_col(d, d.n_layers);
     L.work_col = col;
     L.work_stride = al(d.enc_width > 64u ? d.enc_width : 64u, 32);
     col += (uint32_t)G * L.work_stride;
@@ -174,7 +175,7 @@ __device__ __forceinline__ void issue_job(const ModelDesc& d, const TrainLayout&
                            k > 0 ? 1u : 0u);
     }
     // weight gradient over the tile's rows (both operands MN-major, K = rows)
-    const uint32_t dw = tmem + L.dw_col[b];
+    const uint32_t dw = tmem + dw_col(d, b);
     const bool started = (dw_started >> b) & 1u;
     dw_started |= 1u << b;
     if (last) {
@@ -196,7 +197,7 @@ __device__ __forceinline__ void issue_job(const ModelDesc& d, const TrainLayout&
     }
 }
 
-template <typename T, int G, int NL>
+template <typename T, int G>
 __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_constant__ ModelDesc d, const __grid_constant__ TrainTcArgs a,
                                                               uint32_t* __restrict__ status) {
     using Op = tc::OpType<T>;
@@ -212,7 +213,7 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
     float* red = reinterpret_cast<float*>(smem + L.red_off);
 
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t nl = d.n_layers, nh = nl - 1;
+    const uint32_t nl = d.n_layers;
     const uint32_t n_tiles = a.n / kTile;
 
     if (tid == 0) {
@@ -308,15 +309,13 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
         uint8_t* x0 = grp;
         uint8_t* dzb = grp + L.dz_rel;
         auto hbuf = [&](uint32_t i) { return grp + L.h_rel + (i - 1u) * kHBytes; };
-        float* in_s = reinterpret_cast<float*>(hbuf(nh));   // staging aliases the last hidden buffer
-        const uint32_t in_ld = d.n_input + 1;
         const uint32_t row = quarter * 32u + lane;
         const uint32_t taddr = tmem + L.work_col + grp_i * L.work_stride + ((quarter * 32u) << 16);
         uint32_t dpar = 0, xpar = 0;
         bool x_pending = false;   // a bulk copy of X0 is in flight (thread gtid 0)
         const uint32_t x0_bytes = kTile * d.enc_width * 2u;
         const uint8_t* enc_tiles = reinterpret_cast<const uint8_t*>(a.enc_tiles);
-        if (enc_tiles && gtid == 0 && first_tile + grp_i < n_tiles) {
+        if (gtid == 0 && first_tile + grp_i < n_tiles) {
             tc::mbar_arrive_expect_tx(&xbar[grp_i], x0_bytes);
             tc::bulk_copy_g2s(x0, enc_tiles + (size_t)(first_tile + grp_i) * x0_bytes, x0_bytes, &xbar[grp_i]);
             x_pending = true;
@@ -324,28 +323,16 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
 
         for (uint32_t tile = first_tile + grp_i; tile < n_tiles; tile += stride) {
             const uint32_t row0 = tile * kTile;
-            if (enc_tiles) {
+            {
                 // X0 was encoded by k_encode_tiles; its copy was issued when the previous tile's
                 // last MMA job had finished reading X0.
                 const bool ok = gtid != 0 || tc::mbar_wait_bounded(&xbar[grp_i], xpar, kWaitCycles);
                 x_pending = x_pending && !ok;
-                xpar ^= ok ? 1u : 0u;
+                xpar ^= 1u;
                 if (group_sync_or(bar_id, !ok)) {
                     aborted = true;
                     break;
                 }
-            } else {
-                const float* in_tile = a.in + (size_t)row0 * d.n_input;
-                for (uint32_t idx = gtid; idx < kTile * d.n_input; idx += kGT) {
-                    const uint32_t r = idx / d.n_input, c = idx - r * d.n_input;
-                    in_s[r * in_ld + c] = __ldg(in_tile + idx);
-                }
-                group_sync(bar_id);
-                TcStore<T> st{x0, d.enc_width * 16u};
-                encode_tile_rows<NL>(d, lvl_s, a.params, in_s, in_ld, a.max_level_gpu, a.max_level, row0, kTile, gtid, kGT, st);
-                tc::fence_proxy_async_smem();
-                tc::fence_before_sync();
-                group_sync(bar_id);
             }
             if (gtid == 0) tc::mbar_arrive(&ready[grp_i]);
 
@@ -403,7 +390,7 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
                     }
                 } else {
                     const uint32_t b = 2u * nl - 1u - j;
-                    if (b == 0 && enc_tiles && gtid == 0 && tile + stride < n_tiles) {
+                    if (b == 0 && gtid == 0 && tile + stride < n_tiles) {
                         // every MMA reading X0 has completed: fetch the next tile during this epilogue
                         tc::mbar_arrive_expect_tx(&xbar[grp_i], x0_bytes);
                         tc::bulk_copy_g2s(x0, enc_tiles + (size_t)(tile + stride) * x0_bytes, x0_bytes, &xbar[grp_i]);
@@ -448,18 +435,15 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
                             float* gtab = a.grads + gd.param_offset;
                             uint32_t p0, p1, p2;
                             hash_primes(gd.hash, p0, p1, p2);
-                            for (uint32_t l0 = 0; l0 < gd.n_levels; l0 += 8) {
-                                uint32_t r[16];
-                                tc::tmem_ld16(taddr + s.out_begin + 2u * l0, r);
-                                tc::tmem_wait_ld();
 #pragma unroll 1
-                                for (uint32_t q = 0; q < 8 && l0 + q < gd.n_levels; ++q) {
-                                    const uint32_t level = l0 + q;
-                                    const bool act = !grid_level_skipped_backward(level, ml, gd.n_levels);
-                                    const float2 dy = make_float2(__uint_as_float(r[2 * q]) * a.grad_scale, __uint_as_float(r[2 * q + 1]) * a.grad_scale);
-                                    if (gd.interp == INTERP_NEAREST) grid_level_backward(gd, level, gtab, px, py, pz, dy, act);
-                                    else grid_level_scatter8<kScatterAggregate>(gd, lv[level], gtab, p0, p1, p2, px, py, pz, dy, act);
-                                }
+                            for (uint32_t level = 0; level < gd.n_levels; ++level) {
+                                uint32_t r0, r1;
+                                tc::tmem_ld2(taddr + s.out_begin + 2u * level, r0, r1);
+                                tc::tmem_wait_ld();
+                                const bool act = !grid_level_skipped_backward(level, ml, gd.n_levels);
+                                const float2 dy = make_float2(__uint_as_float(r0) * a.grad_scale, __uint_as_float(r1) * a.grad_scale);
+                                if (gd.interp == INTERP_NEAREST) grid_level_backward(gd, level, gtab, px, py, pz, dy, act);
+                                else grid_level_scatter8<kScatterAggregate>(gd, lv[level], gtab, p0, p1, p2, px, py, pz, dy, act);
                             }
                         }
                     }
@@ -493,7 +477,7 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
             float* gw = a.grads + d.layer_offset[b];
             for (uint32_t c0 = 0; c0 < ncols; c0 += 16) {
                 uint32_t r[16];
-                tc::tmem_ld16(tmem + L.dw_col[b] + c0 + ((quarter * 32u) << 16), r);
+                tc::tmem_ld16(tmem + dw_col(d, b) + c0 + ((quarter * 32u) << 16), r);
                 tc::tmem_wait_ld();
                 if (lane < 16) {
 #pragma unroll
@@ -531,7 +515,7 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
 // brings it in.  Full occupancy (128-thread CTAs) for the gather-bound grid levels.
 template <typename T, int NL>
 __global__ void __launch_bounds__(kTile) k_encode_tiles(const __grid_constant__ ModelDesc d, const __grid_constant__ TrainTcArgs a) {
-    extern __shared__ __align__(16) uint8_t smem[];
+    extern __shared__ __align__(1024) uint8_t smem[];
     GridLevel* lvl_s = reinterpret_cast<GridLevel*>(smem);
     float* in_s = reinterpret_cast<float*>(smem + kMaxGrids * kMaxLevels * sizeof(GridLevel));
     const uint32_t tid = threadIdx.x;
@@ -574,7 +558,7 @@ bool layout_ok(const ModelDesc& d, int G) {
     return L.total <= kMaxSmem && L.tmem_cols <= 512u;
 }
 
-template <typename T, int G, int NL>
+template <typename T, int G>
 cudaError_t launch_g(const ModelDesc& d, const TrainTcArgs& a, uint32_t* status, cudaStream_t s) {
     const TrainLayout L = train_layout(d, G);
     const uint32_t n_tiles = a.n / kTile;
@@ -582,18 +566,18 @@ cudaError_t launch_g(const ModelDesc& d, const TrainTcArgs& a, uint32_t* status,
     const uint32_t need = (n_tiles + G - 1) / G;
     if (blocks > need) blocks = need;
     if (blocks == 0) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_train_tc<T, G, NL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+    cudaError_t e = cudaFuncSetAttribute(k_train_tc<T, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
     if (e != cudaSuccess) return e;
-    k_train_tc<T, G, NL><<<blocks, G * kGT + 32, L.total, s>>>(d, a, status);
+    k_train_tc<T, G><<<blocks, G * kGT + 32, L.total, s>>>(d, a, status);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_t(const ModelDesc& d, const TrainTcArgs& a, int G, uint32_t* status, cudaStream_t s) {
     switch (G) {
-        case 2: return launch_g<T, 2, 2>(d, a, status, s);
-        case 3: return launch_g<T, 3, 2>(d, a, status, s);
-        case 4: return launch_g<T, 4, 2>(d, a, status, s);
+        case 2: return launch_g<T, 2>(d, a, status, s);
+        case 3: return launch_g<T, 3>(d, a, status, s);
+        case 4: return launch_g<T, 4>(d, a, status, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -626,7 +610,7 @@ cudaError_t launch_encode_tiles(const ModelDesc& d, const TrainTcArgs& a, int ki
 }
 
 cudaError_t launch_train_tc(const ModelDesc& d, const TrainTcArgs& a, int kind, int G, uint32_t* status, cudaStream_t s) {
-    if (G < 2 || G > 4 || !layout_ok(d, G)) return cudaErrorInvalidValue;
+    if (G < 2 || G > 4 || !layout_ok(d, G) || !a.enc_tiles) return cudaErrorInvalidValue;
     if (kind == 1) return launch_t<__half>(d, a, G, status, s);
     if (kind == 2) return launch_t<__nv_bfloat16>(d, a, G, status, s);
     return cudaErrorInvalidValue;
