@@ -306,23 +306,47 @@ def main():
         vis[prec] = nv / (statistics.mean(tv) * 1e-3)
         del mv
 
-    # ---- visibility training step, batch 2^18 ----
+    # ---- training steps: visibility (2^18, BCE) and throughput (2^20, RelativeL2, EMA/decay Adam) ----
+    def train_times(enc_, net_, n_in, n_out, loss, opt, x_np, t_np, seed, precs):
+        sp = oracle.model_spec(enc_, net_, n_in, n_out)
+        pr = W.xavier_params(sp, seed=seed)
+        xd_, td_ = torch.from_numpy(x_np).to(dev), torch.from_numpy(t_np).to(dev)
+        res = {}
+        for prec in precs:
+            mt = NetworkWithInputEncoding(n_in, n_out, enc_, net_, loss=loss, optimizer=opt, precision=prec)
+            mt.set_params(pr)
+            lo = torch.empty(1, device=dev)
+            steps = max(3, args.steps // 2) if prec != "fp32" else max(3, args.steps // 4)
+            tr = time_steps(lambda: mt.training_step(xd_, td_, lo), steps, 3, flush)
+            mt.sync_status()
+            res[prec] = statistics.mean(tr)
+            del mt
+        return res
+
     nt = W.WORKLOADS["visibility_train"]["batch"]
     tenc, tnet = W.visibility_configs(16)
-    tspec = oracle.model_spec(tenc, tnet, 6, 1)
-    tparams = W.xavier_params(tspec, seed=9)
     xt, _, _ = W.visibility_inputs(nt, seed=3)
     tt = (np.random.default_rng(3).random((nt, 1)) < 0.3).astype(np.float32)
-    xtd, ttd = torch.from_numpy(xt).to(dev), torch.from_numpy(tt).to(dev)
-    train = {}
-    for prec in ("fp16", "fp32"):
-        mt = NetworkWithInputEncoding(6, 1, tenc, tnet, loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER,
-                                      precision=prec)
-        mt.set_params(tparams)
-        lo = torch.empty(1, device=dev)
-        tr = time_steps(lambda: mt.training_step(xtd, ttd, lo), max(3, args.steps // 2), 3, flush)
-        train[prec] = nt / (statistics.mean(tr) * 1e-3)
-        del mt
+    train = train_times(tenc, tnet, 6, 1, W.VISIBILITY_LOSS, W.VISIBILITY_OPTIMIZER, xt, tt, 9, ("fp16", "bf16", "fp32"))
+    ntt = 1 << 20
+    henc, hnet = W.throughput_configs()
+    xh = W.throughput_inputs(ntt, seed=4)
+    th = np.random.default_rng(4).random((ntt, 3)).astype(np.float32)
+    ttrain = train_times(henc, hnet, 10, 3, W.THROUGHPUT_LOSS, W.THROUGHPUT_OPTIMIZER, xh, th, 10, ("fp16", "bf16", "fp32"))
+
+    # ---- voxelization of the 2.0M-triangle scene at 1024^3 ----
+    from neural_lod_gb300 import voxelize as V
+    mesh = torch.from_numpy(W.synthetic_mesh()).to(dev)
+    vmin, vmax = V.mesh_bounds(mesh)
+    vb, _, vu = V.mesh_frame(vmin, vmax, 1024)
+    vbits = torch.zeros(V.n_words(1024), dtype=torch.int32, device=dev)
+
+    def vox_step():
+        vbits.zero_()
+        V.voxelize(mesh, 1024, vb, vu, out=vbits)
+
+    tvox = statistics.mean(time_steps(vox_step, max(3, args.steps // 2), 3, flush))
+    del mesh, vbits
 
     # ---- aggregate over ranks ----
     total_queries = n * world
@@ -359,8 +383,17 @@ def main():
         "speedup_fp16_vs_fp32": ms32 / ms16,
         "err_vs_fp64": {"fp16_mean_abs": err16, "fp32_mean_abs": err32, "sample": ns},
         "visibility_query": {"batch": nv, "fp16_queries_per_s": vis["fp16"], "fp32_queries_per_s": vis["fp32"]},
-        "visibility_train": {"batch": nt, "fp16_samples_per_s": train["fp16"], "fp32_samples_per_s": train["fp32"],
-                             "flop_per_sample": TRAIN_FLOP_PER_SAMPLE},
+        "visibility_train": {"batch": nt, "unit": "samples/s", "flop_per_sample": TRAIN_FLOP_PER_SAMPLE,
+                             **{f"{p}_samples_per_s": nt / (t * 1e-3) for p, t in train.items()},
+                             **{f"{p}_ms_per_step": t for p, t in train.items()},
+                             "speedup_fp16_vs_fp32": train["fp32"] / train["fp16"]},
+        "throughput_train": {"batch": ntt, "unit": "samples/s", "flop_per_sample": 3 * FLOP_PER_QUERY,
+                             "optimizer": "Ema(0.95) of ExponentialDecay(Adam lr 5e-3)", "loss": "RelativeL2",
+                             **{f"{p}_samples_per_s": ntt / (t * 1e-3) for p, t in ttrain.items()},
+                             **{f"{p}_ms_per_step": t for p, t in ttrain.items()},
+                             "speedup_fp16_vs_fp32": ttrain["fp32"] / ttrain["fp16"]},
+        "voxelize": {"triangles": 2_000_000, "grid": 1024, "ms": tvox, "triangles_per_s": 2e6 / (tvox * 1e-3),
+                     "scene": "20k ellipsoid shells (48 tris) + 0.52M quads, unit cube, 1e-4 padding"},
         "clocks": clocks,
         "gpu_launches": len(times16),
         "kernel_variant": variant,
