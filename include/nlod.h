@@ -155,7 +155,9 @@ NLOD_API int nlod_training_step(nlod_module* m, void* stream, uint32_t n, const 
  * nlod_training_step for callers that cannot allocate device memory while they train, for example
  * an online learner that takes one step inside a real-time frame loop with a no-allocation budget.
  * No counterpart in the reference (tiny-cuda-nn's Trainer allocates its step workspace from its
- * memory arena).  Same arguments, result and status codes as nlod_training_step; the step's
+ * memory arena).  Same arguments and status codes as nlod_training_step; the step runs the plain
+ * FP32 kernels whatever precision the module has (the tensor-core step needs a workspace of its
+ * own), so its result is that of nlod_training_step on the module's FP32 form.  The step's
  * intermediates live in a fixed 16 MiB device scratch that the library holds on every GPU that uses
  * it until the process exits, instead of a cudaMalloc'ed workspace, and the call itself allocates
  * nothing.  A batch whose intermediates do not fit is rejected with NLOD_ERR_INVALID and a message

@@ -1,6 +1,7 @@
 """nlod_training_step_noalloc: the training step for callers that cannot allocate device memory
-while they train (for example an online learner inside a real-time frame loop).  It must give the
-same result as nlod_training_step, call after call, from its fixed scratch instead of a
+while they train (for example an online learner inside a real-time frame loop).  It runs the plain
+FP32 step whatever precision the module was created with, so it must give the same result as
+nlod_training_step on the module's FP32 form, call after call, from its fixed scratch instead of a
 cudaMalloc'ed workspace.  Both entry points are called through the C ABI.
 
 This file is named so that pytest collects it last."""
@@ -19,7 +20,8 @@ def _rel(a, b):
     return float(np.linalg.norm(a.astype(np.float64) - b) / max(np.linalg.norm(b.astype(np.float64)), 1e-30))
 
 
-def test_training_step_noalloc_matches_training_step(cuda, nlod_lib):
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_training_step_noalloc_matches_training_step(cuda, nlod_lib, precision):
     import torch
 
     enc, net = W.visibility_configs(16)
@@ -29,8 +31,8 @@ def test_training_step_noalloc_matches_training_step(cuda, nlod_lib):
     x, _, _ = W.visibility_inputs(n, seed=22)
     t = (np.random.default_rng(23).random((n, 1)) < 0.4).astype(np.float32)
     xd, td = torch.from_numpy(x).to(cuda), torch.from_numpy(t).to(cuda)
-    ref = NetworkWithInputEncoding(6, 1, enc, net, loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER, precision="fp16")
-    noa = NetworkWithInputEncoding(6, 1, enc, net, loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER, precision="fp16")
+    ref = NetworkWithInputEncoding(6, 1, enc, net, loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER, precision="fp32")
+    noa = NetworkWithInputEncoding(6, 1, enc, net, loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER, precision=precision)
     ref.set_params(params)
     noa.set_params(params)
     loss_ref = torch.zeros(1, device=cuda)
