@@ -269,6 +269,50 @@ NLOD_API int nlod_mesh_frame(const float mesh_min[3], const float mesh_max[3], u
 NLOD_API int nlod_voxelize(const float* triangles, uint64_t n_triangles, uint32_t grid, const float bbox_min[3],
                            const float unit[3], uint32_t* bits, void* stream);
 
+/* ---- Wavefront render query ---------------------------------------------------------------------
+ * Pinhole rays through one level of the LoD pyramid: every occupied voxel a ray enters is one
+ * visibility query; an accepted voxel (visibility >= threshold) is one throughput query and a
+ * bounce in a uniformly sampled direction; rays that leave the grid take the background (before
+ * any bounce) or throughput x environment radiance.  This is the reference's wavefront loop
+ * (rptr/cuda/neural-lod/wavefront_neural_throughput_visibility_lod.cu:470-720 with the per-ray
+ * steps of rptr/cuda/wavefront_neural_pt.cuh: raymarch_impl, generate_*_inference_data_impl,
+ * check_visibility, process_ray_bounce) without the host round trip per wavefront: a frame is one
+ * CUDA-graph launch whose rounds run in a conditional while node.
+ * Network inputs: visibility = (voxel-local entry point in [0,1]^3, (dir + 1) / 2) with
+ * lod_max_level as the grid's max level; throughput = (voxel centre / res, (wi + 1) / 2,
+ * (wo + 1) / 2, lod_input), wo = -dir.  Camera and radiance parameters are the renderer's. */
+typedef struct nlod_renderer nlod_renderer;
+typedef struct nlod_render_params {
+    uint32_t width, height;        /* pixels (one ray per pixel) */
+    uint32_t level;                /* pyramid level the rays traverse */
+    uint32_t max_depth;            /* path vertices; a hit on the last one ends the path dark (reference: 4) */
+    uint32_t max_vis_queries;      /* visibility queries per ray and bounce before the path is dropped */
+    float threshold;               /* visibility >= threshold accepts the voxel */
+    float eye[3], target[3], up[3];  /* camera in the grid's normalised coordinates [0,1]^3 */
+    float fov_y_deg;
+    float background[3];           /* radiance of rays that escape before the first bounce */
+    float env_color[3];            /* radiance (times throughput) of rays that escape after one */
+    float lod_max_level;           /* visibility network's max grid level fraction for this LoD */
+    float lod_input;               /* throughput network's LoD input column for this LoD */
+    uint64_t seed;                 /* direction sampling */
+} nlod_render_params;
+
+/* Index-space camera of a level with res voxels per axis: eye[3], right[3] (scaled by
+ * tan(fov/2) * aspect), up[3] (scaled by tan(fov/2)), forward[3].  Host only. */
+NLOD_API int nlod_render_camera(const nlod_render_params* p, uint32_t level_res, float* out12);
+/* Builds the frame graph (allocates the ray state and query buffers); the modules and the grid
+ * must outlive the renderer.  Synchronous. */
+NLOD_API int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const nlod_lod_grid* grid,
+                                  const nlod_render_params* p, nlod_renderer** out);
+NLOD_API void nlod_renderer_destroy(nlod_renderer* r);
+/* Renders one frame: image [height][width][3] FP32 device (NULL to skip the copy), ray_stats
+ * [height*width][2] visibility / throughput queries per ray (NULL to skip).  Asynchronous. */
+NLOD_API int nlod_render_frame(nlod_renderer* r, void* stream, float* image, uint32_t* ray_stats);
+/* Totals of the last frame: visibility queries, throughput queries, rounds, rays dropped at the
+ * per-bounce cap.  Synchronises; NLOD_ERR_TIMEOUT if a ray ran out of DDA steps or the frame hit
+ * its round bound. */
+NLOD_API int nlod_render_stats(nlod_renderer* r, void* stream, uint64_t* out4);
+
 #ifdef __cplusplus
 }
 #endif

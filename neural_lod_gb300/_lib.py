@@ -72,6 +72,11 @@ SIGNATURES = [
     ("nlod_mesh_bounds", C.c_int, [_fp, C.c_uint64, _vp, _fp, _fp]),
     ("nlod_mesh_frame", C.c_int, [_fp, _fp, _u32, C.c_float, _fp, _fp, _fp]),
     ("nlod_voxelize", C.c_int, [_fp, C.c_uint64, _u32, _fp, _fp, _fp, _vp]),
+    ("nlod_render_camera", C.c_int, [_vp, _u32, _fp]),
+    ("nlod_renderer_create", C.c_int, [_vp, _vp, _vp, _vp, C.POINTER(_vp)]),
+    ("nlod_renderer_destroy", None, [_vp]),
+    ("nlod_render_frame", C.c_int, [_vp, _vp, _fp, _fp]),
+    ("nlod_render_stats", C.c_int, [_vp, _vp, _fp]),
 ]
 
 _lib = None

@@ -247,6 +247,25 @@ void init_params(nlod_module* m, uint64_t seed) {
 
 }  // namespace
 
+namespace nlod {
+
+// Inference launch used by the wavefront renderer: inference parameters, a scalar max level, and
+// the row count read from device memory at launch time (n_max rows of input/output storage).
+cudaError_t module_inference_device_count(nlod_module* m, uint32_t n_max, const float* in, float* out, const uint32_t* n_dev,
+                                          float max_level, cudaStream_t s) {
+    ForwardArgs a = base_forward_args(m, n_max, in, true);
+    a.out = out;
+    a.n_dev = n_dev;
+    a.max_level_gpu = nullptr;
+    a.max_level = max_level;
+    if (m->precision == NLOD_PRECISION_FP32) return launch_forward_simt(m->d, a, 0, s);
+    return launch_forward_tc(m->d, a, m->op_kind(), m->tc_variant, m->status, s);
+}
+
+uint32_t* module_status_word(nlod_module* m) { return m->status; }
+
+}  // namespace nlod
+
 extern "C" {
 
 const char* nlod_last_error(void) { return g_last_error.c_str(); }

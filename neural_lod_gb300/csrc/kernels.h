@@ -29,7 +29,17 @@ struct ForwardArgs {
     float loss_scale;
     float* dz;                        // [n][16] dL/d(pre-activation output) * loss_scale
     float* loss_partial;              // [gridDim.x] per-block loss sums (mean-normalised)
+    // inference only: when set, the rows to process are min(n, *n_dev rounded up to 128); rows
+    // past *n_dev inside the last tile are computed from whatever the input holds and ignored
+    const uint32_t* n_dev;
 };
+
+// Rows an inference launch processes (n, or the device-side count when given).
+__device__ __forceinline__ uint32_t forward_rows(const ForwardArgs& a) {
+    if (!a.n_dev) return a.n;
+    const uint32_t c = (*a.n_dev + 127u) & ~127u;
+    return c < a.n ? c : a.n;
+}
 
 // Plain FP32 form.
 cudaError_t launch_forward_simt(const ModelDesc& d, const ForwardArgs& a, int n_blocks_hint, cudaStream_t s);
@@ -128,7 +138,7 @@ struct TrainTcArgs {
     float* grads;                     // FP32 gradient vector
     float* loss_partial;              // [gridDim.x] per-CTA loss sums (nullable)
     void* enc_tiles;                  // [n/128][128 x enc_width] operand-type X0 tiles written by
-                                      // launch_encode_tiles; nullable (the fused kernel then encodes)
+                                      // launch_encode_tiles and bulk-copied by the fused kernel
 };
 // Tile pipelines per CTA that fit the network (0 = network not supported by the fused kernel).
 int train_tc_groups(const ModelDesc& d);

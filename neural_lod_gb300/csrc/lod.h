@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 namespace nlod {
 
@@ -28,3 +29,13 @@ cudaError_t launch_first_active_voxel(const LodLevelDev& L, uint32_t n, const fl
                                       uint32_t* status, cudaStream_t s);
 
 }  // namespace nlod
+
+// The C ABI's pyramid object (include/nlod.h): one LodLevelDev per level plus owned buffers.
+struct nlod_lod_grid {
+    uint32_t n_levels = 0;
+    int32_t res0 = 0;
+    nlod::LodLevelDev levels[nlod::kMaxLodLevels]{};
+    uint32_t n_leaves[nlod::kMaxLodLevels]{};
+    std::vector<void*> owned;
+    uint32_t* status = nullptr;
+};

@@ -14,15 +14,6 @@
 
 using namespace nlod;
 
-struct nlod_lod_grid {
-    uint32_t n_levels = 0;
-    int32_t res0 = 0;
-    LodLevelDev levels[kMaxLodLevels]{};
-    uint32_t n_leaves[kMaxLodLevels]{};
-    std::vector<void*> owned;
-    uint32_t* status = nullptr;
-};
-
 extern "C" {
 
 void nlod_lod_grid_destroy(nlod_lod_grid* g) {

@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kThreads) k_forward_simt(const __grid_constant
     float* w_s = smem + L.off_w;
     float* red_s = smem + L.off_red;
 
-    const uint32_t n_tiles = a.n / kTile;
+    const uint32_t n_tiles = forward_rows(a) / kTile;
     const float inv_n_total = 1.0f / ((float)a.n * (float)d.n_output);
     float loss_acc = 0.f;
 

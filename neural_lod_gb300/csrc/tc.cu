@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
 
     uint32_t phase = 0;
     bool aborted = false;
-    const uint32_t n_tiles = a.n / kTcTile;
+    const uint32_t n_tiles = forward_rows(a) / kTcTile;
     const uint32_t row = quarter * 32u + lane;   // TMEM lane == tile row owned in the epilogue
     const uint32_t taddr_row = tmem_base + ((quarter * 32u) << 16);
 

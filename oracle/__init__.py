@@ -74,6 +74,8 @@ def declare(L):
     L.orc_lod_level.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp, vp]
     L.orc_first_active_voxel_batch.restype = None
     L.orc_first_active_voxel_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.orc_render.restype = None
+    L.orc_render.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.orc_mesh_frame.restype = None
     L.orc_mesh_frame.argtypes = [vp, vp, C.c_uint32, f32, vp, vp, vp]
     L.orc_voxelize.restype = None
@@ -235,6 +237,33 @@ class LodLevel:
         return hit, ijk, tn, tf
 
 
+class OrcRenderParams(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("max_depth", C.c_uint32), ("max_vis", C.c_uint32),
+                ("threshold", C.c_float), ("lod_max_level", C.c_float), ("lod_input", C.c_float),
+                ("background", C.c_float * 3), ("env", C.c_float * 3), ("seed", C.c_uint64)]
+
+
+def render(vis: "Oracle", vis_params, thr: "Oracle", thr_params, level: "LodLevel", params, cam):
+    """Wavefront render restated on the host: returns (image [h,w,3] float32, ray_stats [h*w,2]
+    uint32, totals (visibility queries, throughput queries, dropped rays)).  `params` has the
+    fields of neural_lod_gb300.render.RenderParams; cam = the renderer's 12-float camera."""
+    p = OrcRenderParams()
+    p.width, p.height, p.max_depth, p.max_vis = params.width, params.height, params.max_depth, params.max_vis_queries
+    p.threshold, p.lod_max_level, p.lod_input, p.seed = params.threshold, params.lod_max_level, params.lod_input, params.seed
+    p.background[:] = list(params.background)
+    p.env[:] = list(params.env_color)
+    n = params.width * params.height
+    image = np.zeros((n, 3), np.float32)
+    stats = np.zeros((n, 2), np.uint32)
+    totals = np.zeros(3, np.uint64)
+    vp_ = np.ascontiguousarray(vis_params, dtype=np.float64)
+    tp_ = np.ascontiguousarray(thr_params, dtype=np.float64)
+    cam = np.ascontiguousarray(cam, dtype=np.float32)
+    lib().orc_render(C.byref(vis.m), vp_.ctypes.data, C.byref(thr.m), tp_.ctypes.data, C.byref(level.s), C.byref(p),
+                     cam.ctypes.data, image.ctypes.data, stats.ctypes.data, totals.ctypes.data)
+    return image.reshape(params.height, params.width, 3), stats, tuple(int(v) for v in totals)
+
+
 def mesh_frame(mesh_min, mesh_max, grid: int, eps: float = 1e-4):
     """createMeshBBCube + voxinfo: (bbox_min, bbox_max, unit), each float32[3]."""
     mn = np.ascontiguousarray(mesh_min, dtype=np.float32)
@@ -262,4 +291,4 @@ def sh(degree: int, x: float, y: float, z: float):
     return np.array(out[:], dtype=np.float64)
 
 
-__all__ = ["Oracle", "LodLevel", "adam_step", "sh", "grid_levels", "model_spec", "mesh_frame", "voxelize"]
+__all__ = ["Oracle", "LodLevel", "adam_step", "sh", "grid_levels", "model_spec", "mesh_frame", "voxelize", "render"]

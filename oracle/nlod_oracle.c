@@ -783,3 +783,110 @@ void orc_first_active_voxel_batch(const OrcLodLevel* L, int64_t n, const float* 
         t_far[i] = hit[i] ? tf : 0.f;
     }
 }
+
+/* ---------------------------------------------------------------------------------------------
+ * Wavefront render query, one ray at a time (restating the renderer of this library, which
+ * follows rptr/cuda/neural-lod/wavefront_neural_throughput_visibility_lod.cu:470-720 and the
+ * per-ray steps of rptr/cuda/wavefront_neural_pt.cuh).  Geometry and sampling in IEEE single
+ * precision without contraction (bit-identical rays), networks in FP64 through orc_forward.
+ * ------------------------------------------------------------------------------------------- */
+static uint32_t orc_mix32(uint32_t h) {
+    h ^= h >> 16; h *= 0x7feb352du; h ^= h >> 15; h *= 0x846ca68bu; h ^= h >> 16;
+    return h;
+}
+static float orc_u01(uint32_t h) { return (float)(h >> 8) * (1.0f / 16777216.0f); }
+
+static void orc_sample_sphere(uint32_t key, float w[3]) {
+    for (uint32_t t = 0; t < 16; ++t) {
+        const uint32_t h = orc_mix32(key + t * 0x632BE5ABu);
+        const float x = 2.f * orc_u01(h) - 1.f;
+        const float y = 2.f * orc_u01(orc_mix32(h ^ 0x68E31DA4u)) - 1.f;
+        const float z = 2.f * orc_u01(orc_mix32(h ^ 0xB5297A4Du)) - 1.f;
+        const float r2 = (x * x + y * y) + z * z;
+        if (r2 <= 1.f && r2 >= 1e-4f) {
+            const float r = sqrtf(r2);
+            w[0] = x / r; w[1] = y / r; w[2] = z / r;
+            return;
+        }
+    }
+    w[0] = 0.f; w[1] = 0.f; w[2] = 1.f;
+}
+
+void orc_render(const OrcModel* vis, const double* vis_params, const OrcModel* thr, const double* thr_params, const OrcLodLevel* L,
+                const OrcRenderParams* p, const float cam[12], float* image, uint32_t* ray_stats, uint64_t* totals) {
+    const int64_t n = (int64_t)p->width * p->height;
+    const uint32_t seed_lo = (uint32_t)p->seed, seed_hi = (uint32_t)(p->seed >> 32);
+    const float res = (float)L->res;
+    uint64_t tv = 0, tt = 0, dropped = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : tv, tt, dropped)
+    for (int64_t ray = 0; ray < n; ++ray) {
+        const uint32_t px = (uint32_t)(ray % p->width), py = (uint32_t)(ray / p->width);
+        const float W = (float)p->width, H = (float)p->height;
+        const float a = (2.f * ((float)px + 0.5f) - W) / W;
+        const float b = (H - 2.f * ((float)py + 0.5f)) / H;
+        float o[3], d[3], dd[3], tp[3] = {1.f, 1.f, 1.f};
+        for (int k = 0; k < 3; ++k) dd[k] = (a * cam[3 + k] + b * cam[6 + k]) + cam[9 + k];
+        const float len = sqrtf((dd[0] * dd[0] + dd[1] * dd[1]) + dd[2] * dd[2]);
+        for (int k = 0; k < 3; ++k) { o[k] = cam[k]; d[k] = dd[k] / len; }
+        int32_t ijk[3] = {-1, -1, -1};
+        float tmin = 0.f;
+        uint32_t bounce = 0, nvis = 0, qv = 0, qt = 0;
+        float* img = image + 3 * ray;
+        img[0] = img[1] = img[2] = 0.f;
+        for (;;) {
+            if (nvis >= p->max_vis) { dropped++; break; }
+            int32_t v[3];
+            float tn = 0.f, tf = 0.f;
+            if (!orc_first_active_voxel(L, o, d, tmin, ijk, v, &tn, &tf)) {
+                for (int k = 0; k < 3; ++k) img[k] = bounce == 0 ? p->background[k] : tp[k] * p->env[k];
+                break;
+            }
+            for (int k = 0; k < 3; ++k) ijk[k] = v[k];
+            ++nvis;
+            ++qv;
+            float in[10];
+            for (int k = 0; k < 3; ++k) {
+                const float pk = o[k] + d[k] * tn;
+                float l = pk - (float)ijk[k];
+                l = l < 0.f ? 0.f : (l > 1.f ? 1.f : l);
+                in[k] = l;
+                in[3 + k] = (d[k] + 1.f) * 0.5f;
+            }
+            double vo;
+            orc_forward(vis, 1, in, vis_params, NULL, p->lod_max_level, &vo, NULL);
+            if (vo >= (double)p->threshold) {
+                if (bounce + 1 >= p->max_depth) break;   /* hit on the last path vertex: dark */
+                float wi[3];
+                orc_sample_sphere(orc_mix32(orc_mix32((uint32_t)ray ^ orc_mix32(seed_lo ^ orc_mix32(seed_hi))) ^ (bounce * 0x9E3779B9u)), wi);
+                for (int k = 0; k < 3; ++k) {
+                    in[k] = ((float)ijk[k] + 0.5f) / res;
+                    in[3 + k] = (wi[k] + 1.f) * 0.5f;
+                    in[6 + k] = (-d[k] + 1.f) * 0.5f;
+                }
+                in[9] = p->lod_input;
+                double to[3];
+                orc_forward(thr, 1, in, thr_params, NULL, 1000.f, to, NULL);
+                ++qt;
+                const float t_eps = tn + 1e-4f * (tf - tn);
+                int alive = 0;
+                for (int k = 0; k < 3; ++k) {
+                    const float tk = (float)to[k];
+                    tp[k] = tp[k] * ((tk > 0.f ? tk : 0.f) * 12.566370614359172f);
+                    alive |= tp[k] != 0.f;
+                    o[k] = o[k] + d[k] * t_eps;
+                    d[k] = wi[k];
+                }
+                tmin = 0.f;
+                ++bounce;
+                nvis = 0;
+                if (!alive) break;
+            } else {
+                tmin = (tn + tf) * 0.5f;
+            }
+        }
+        if (ray_stats) { ray_stats[2 * ray] = qv; ray_stats[2 * ray + 1] = qt; }
+        tv += qv;
+        tt += qt;
+    }
+    if (totals) { totals[0] = tv; totals[1] = tt; totals[2] = dropped; }
+}

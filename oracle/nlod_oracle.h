@@ -144,6 +144,21 @@ void orc_mesh_frame(const float mn[3], const float mx[3], uint32_t grid, float e
  * voxelize_triangle (cuda_voxelizer/src/voxelize.cu:58-190) in IEEE single precision. */
 void orc_voxelize(const float* tris, int64_t n, const float bmin[3], const float unit[3], uint32_t grid, uint32_t* bits);
 
+/* Wavefront render query (see orc_render in nlod_oracle.c). */
+typedef struct {
+    uint32_t width, height, max_depth, max_vis;
+    float threshold, lod_max_level, lod_input;
+    float background[3], env[3];
+    uint64_t seed;
+} OrcRenderParams;
+
+/* Renders width x height rays through level L with the visibility / throughput networks;
+ * cam = index-space eye, right, up, forward (12 floats).  image [n][3]; ray_stats [n][2]
+ * (visibility, throughput queries) or NULL; totals[3] = visibility queries, throughput queries,
+ * rays dropped at the per-bounce cap (or NULL). */
+void orc_render(const OrcModel* vis, const double* vis_params, const OrcModel* thr, const double* thr_params, const OrcLodLevel* L,
+                const OrcRenderParams* p, const float cam[12], float* image, uint32_t* ray_stats, uint64_t* totals);
+
 /* FP32 scalar forward over all host threads: the timed CPU baseline. Returns threads used. */
 int orc_forward_f32(const OrcModel* m, int64_t n, const float* in, const float* params, const float* max_level,
                     float max_level_scalar, float* out, int n_threads);
