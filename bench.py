@@ -348,6 +348,51 @@ def main():
     tvox = statistics.mean(time_steps(vox_step, max(3, args.steps // 2), 3, flush))
     del mesh, vbits
 
+    # ---- wavefront render query: 1024^2 rays, LoD pyramid 512^3 -> 4^3, 4 path vertices ----
+    from neural_lod_gb300.lod import LodGrid
+    from neural_lod_gb300.render import RenderParams, Renderer, camera
+
+    occ = W.value_noise_occupancy(256, seed=5, spacing=16, density=0.3)
+    occ = occ.repeat(2, 0).repeat(2, 1).repeat(2, 2)
+    pyr = LodGrid(W.pack_bits(occ), 512, 8)
+    del occ
+    rlevel = 3
+    rparams = RenderParams(width=1024, height=1024, level=rlevel, max_depth=4, max_vis_queries=64,
+                           lod_max_level=(7 - rlevel) / 8, lod_input=(rlevel + 0.5) / 8, seed=42)
+    venc, vnet = W.visibility_configs()
+    henc, hnet = W.throughput_configs()
+    rv_params = W.xavier_params(oracle.model_spec(venc, vnet, 6, 1), seed=12)
+    rt_params = W.xavier_params(oracle.model_spec(henc, hnet, 10, 3), seed=13)
+    render = {}
+    for prec in ("fp16", "fp32"):
+        rv = NetworkWithInputEncoding(6, 1, venc, vnet, precision=prec)
+        rt = NetworkWithInputEncoding(10, 3, henc, hnet, precision=prec)
+        rv.set_params(rv_params)
+        rt.set_params(rt_params)
+        if prec != "fp32":
+            xa = torch.from_numpy(W.visibility_inputs(1 << 18, seed=6)[0]).to(dev)
+            rv.autotune(xa, torch.empty((1 << 18, 1), device=dev))
+            xb = torch.from_numpy(W.throughput_inputs(1 << 18, seed=6)).to(dev)
+            rt.autotune(xb, torch.empty((1 << 18, 3), device=dev))
+        rr = Renderer(rv, rt, pyr, rparams)
+        frame = torch.empty((1024, 1024, 3), device=dev)
+        ft = time_steps(lambda: rr.frame(frame), max(5, args.steps) if prec != "fp32" else 5, 3, flush)
+        q = rr.stats()
+        ft_sorted = sorted(ft)
+        p50 = ft_sorted[len(ft) // 2]
+        p99 = ft_sorted[min(len(ft) - 1, int(round(0.99 * (len(ft) - 1))))]
+        render[prec] = {"p50_ms": p50, "p99_ms": p99, "frames": len(ft), "vis_queries": q[0], "thr_queries": q[1],
+                        "rounds": q[2], "dropped_rays": q[3], "queries_per_s": (q[0] + q[1]) / (statistics.mean(ft) * 1e-3)}
+        rr.close()
+        del rv, rt
+    # host restatement on a bounded sample of the same frame (FP64 networks, all host threads)
+    rsmall = RenderParams(**{**rparams.__dict__, "width": 96, "height": 96})
+    t0 = time.perf_counter()
+    _, _, rtot = oracle.render(oracle.Oracle(venc, vnet, 6, 1), rv_params, oracle.Oracle(henc, hnet, 10, 3), rt_params,
+                               oracle.LodLevel(pyr.level_bits(rlevel), 512 >> rlevel, 0), rsmall, camera(rsmall, 512 >> rlevel))
+    cpu_render_s = time.perf_counter() - t0
+    del pyr
+
     # ---- aggregate over ranks ----
     total_queries = n * world
     t_step = ms16
@@ -392,6 +437,11 @@ def main():
                              **{f"{p}_samples_per_s": ntt / (t * 1e-3) for p, t in ttrain.items()},
                              **{f"{p}_ms_per_step": t for p, t in ttrain.items()},
                              "speedup_fp16_vs_fp32": ttrain["fp32"] / ttrain["fp16"]},
+        "render": {"workload": "1024x1024 pinhole rays, level 3 (64^3) of a 512^3->4^3 pyramid (256^3 value noise, "
+                               "30% occupied, upsampled x2), 4 path vertices, <= 64 visibility queries per bounce",
+                   "frame": "one CUDA-graph launch (rounds in a conditional while node)", **render,
+                   "cpu_queries_per_s": (rtot[0] + rtot[1]) / cpu_render_s,
+                   "cpu_sample": "96x96 rays of the same camera, FP64 host restatement, all host threads"},
         "voxelize": {"triangles": 2_000_000, "grid": 1024, "ms": tvox, "triangles_per_s": 2e6 / (tvox * 1e-3),
                      "scene": "20k ellipsoid shells (48 tris) + 0.52M quads, unit cube, 1e-4 padding"},
         "clocks": clocks,
