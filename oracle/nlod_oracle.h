@@ -19,9 +19,11 @@
  * same table entries.  Spherical harmonics are evaluated by the associated-Legendre recurrence,
  * independently of the generated polynomials the kernels use.
  *
- * Pinning: layout rules and SH values are checked against fixtures generated from the
- * reference sources (tests/golden/make_golden.py); gradients are checked against FP64 central
- * finite differences of this oracle's own forward.
+ * Pinning: SH values against the reference's own kernel_sh polynomials (tests/golden/
+ * make_sh_golden.py -> sh_golden.npz); grid sizes against the reference's offset-table sizes of the
+ * three workload configurations; the DDA against NanoVDB compiled from the reference tree
+ * (oracle/build_ref.py, tests/golden/make_dda_golden.py); gradients against FP64 central finite
+ * differences of this oracle's own forward.
  */
 #ifndef NLOD_ORACLE_H
 #define NLOD_ORACLE_H

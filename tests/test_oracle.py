@@ -15,6 +15,17 @@ from neural_lod_gb300 import workloads as W
 ROOT = Path(__file__).resolve().parents[1]
 
 
+def test_sh_matches_reference_polynomials_golden():
+    """oracle.sh (associated-Legendre recurrence) against the 64 polynomials of the reference's
+    kernel_sh, evaluated by tests/golden/make_sh_golden.py from spherical_harmonics.h."""
+    from pathlib import Path
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "sh_golden.npz")
+    for d, v in zip(g["dirs"], g["values"]):
+        for degree in (1, 2, 4, 8):
+            np.testing.assert_allclose(oracle.sh(degree, *d), v[: degree * degree], rtol=0, atol=1e-12)
+
+
 def test_sh_recurrence_matches_generated_polynomials():
     src = (ROOT / "neural_lod_gb300" / "csrc" / "sh_basis.inc").read_text()
     exprs = {int(m.group(1)): m.group(2) for m in re.finditer(r"OUT\((\d+), \((.*?)\)\); \\", src)}
