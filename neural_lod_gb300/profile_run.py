@@ -2,6 +2,8 @@
 
     python -m neural_lod_gb300.profile_run query  [--precision fp16] [--n 2097152] [--iters 3]
     python -m neural_lod_gb300.profile_run train  [--precision fp16] [--n 262144]  [--iters 3]
+    python -m neural_lod_gb300.profile_run render [--precision fp16] [--iters 3]
+    python -m neural_lod_gb300.profile_run voxelize [--iters 3]
 
 `query` runs the throughput-query forward (the bench's headline kernel) `iters` times on the
 bench's inputs; `train` runs visibility training steps.  Each run ends with a status check, so a
@@ -18,7 +20,7 @@ sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["query", "train", "visq"])
+    ap.add_argument("what", choices=["query", "train", "visq", "render", "voxelize"])
     ap.add_argument("--precision", default="fp16")
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--iters", type=int, default=3)
@@ -58,6 +60,37 @@ def main():
         out = torch.empty((n, 1), device=dev)
         for _ in range(a.iters):
             m.inference(x, out)
+    elif a.what == "render":
+        from neural_lod_gb300.lod import LodGrid
+        from neural_lod_gb300.render import RenderParams, Renderer
+
+        occ = W.value_noise_occupancy(256, seed=5, spacing=16, density=0.3)
+        pyr = LodGrid(W.pack_bits(occ.repeat(2, 0).repeat(2, 1).repeat(2, 2)), 512, 8)
+        venc, vnet = W.visibility_configs()
+        henc, hnet = W.throughput_configs()
+        rv = N.NetworkWithInputEncoding(6, 1, venc, vnet, precision=a.precision)
+        rt = N.NetworkWithInputEncoding(10, 3, henc, hnet, precision=a.precision)
+        import oracle
+
+        rv.set_params(W.xavier_params(oracle.model_spec(venc, vnet, 6, 1), seed=12))
+        rt.set_params(W.xavier_params(oracle.model_spec(henc, hnet, 10, 3), seed=13))
+        p = RenderParams(width=1024, height=1024, level=3, lod_max_level=4 / 8, lod_input=3.5 / 8, seed=42)
+        r = Renderer(rv, rt, pyr, p)
+        for _ in range(a.iters):
+            r.frame()
+        print("stats", r.stats())
+        n = p.width * p.height
+        m = rv
+    elif a.what == "voxelize":
+        from neural_lod_gb300 import voxelize as V
+
+        mesh = torch.from_numpy(W.synthetic_mesh()).to(dev)
+        for _ in range(a.iters):
+            bits = V.voxelize(mesh, 1024)
+        n = mesh.shape[0]
+        torch.cuda.synchronize()
+        print("ok voxelize", n)
+        return
     else:
         n = a.n or W.WORKLOADS["visibility_train"]["batch"]
         enc, net = W.visibility_configs(16)
