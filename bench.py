@@ -323,10 +323,15 @@ def main():
             del mt
         return res
 
+    from neural_lod_gb300 import samples as S
+    from neural_lod_gb300.lod import LodGrid
+
     nt = W.WORKLOADS["visibility_train"]["batch"]
     tenc, tnet = W.visibility_configs(16)
-    xt, _, _ = W.visibility_inputs(nt, seed=3)
-    tt = (np.random.default_rng(3).random((nt, 1)) < 0.3).astype(np.float32)
+    noise256 = W.value_noise_occupancy(256, seed=5, spacing=16, density=0.3)
+    grid256 = LodGrid(W.pack_bits(noise256), 256, 8)
+    xt, _, tt = S.visibility_batch(grid256, nt, seed=3)     # exact-DDA segment transmittance targets
+    del grid256
     train = train_times(tenc, tnet, 6, 1, W.VISIBILITY_LOSS, W.VISIBILITY_OPTIMIZER, xt, tt, 9, ("fp16", "bf16", "fp32"))
     ntt = 1 << 20
     henc, hnet = W.throughput_configs()
@@ -334,7 +339,7 @@ def main():
     th = np.random.default_rng(4).random((ntt, 3)).astype(np.float32)
     ttrain = train_times(henc, hnet, 10, 3, W.THROUGHPUT_LOSS, W.THROUGHPUT_OPTIMIZER, xh, th, 10, ("fp16", "bf16", "fp32"))
 
-    # ---- voxelization of the 2.0M-triangle scene at 1024^3 ----
+    # ---- voxelize + train: 2.0M triangles at 1024^3, pyramid, exact-DDA targets, 1,000 steps at 2^20 ----
     from neural_lod_gb300 import voxelize as V
     mesh = torch.from_numpy(W.synthetic_mesh()).to(dev)
     vmin, vmax = V.mesh_bounds(mesh)
@@ -346,14 +351,48 @@ def main():
         V.voxelize(mesh, 1024, vb, vu, out=vbits)
 
     tvox = statistics.mean(time_steps(vox_step, max(3, args.steps // 2), 3, flush))
-    del mesh, vbits
+    vox_step()
+    del mesh
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    grid1024 = LodGrid(vbits, 1024, 8)
+    torch.cuda.synchronize()
+    t_pyr = time.perf_counter() - t0
+    n4 = 1 << 20
+    n_batches = 2
+    batches = [S.throughput_batch(grid1024, n4, seed=100 + b) for b in range(n_batches)]
+    del grid1024, vbits
+    xb = [torch.from_numpy(x_).to(dev) for x_, _ in batches]
+    tb = [torch.from_numpy(t_).to(dev) for _, t_ in batches]
+    x_eval = batches[0][0][:4096]
+    e2e4 = {}
+    n_steps4 = 1000
+    for prec in ("fp16", "bf16", "fp32"):
+        m4 = NetworkWithInputEncoding(10, 3, henc, hnet, loss=W.THROUGHPUT_LOSS, optimizer=W.THROUGHPUT_OPTIMIZER, precision=prec,
+                                      seed=11)
+        lo = torch.empty(1, device=dev)
+        losses = []
+        s0, s1 = torch.cuda.Event(True), torch.cuda.Event(True)
+        torch.cuda.synchronize()
+        s0.record()
+        for i in range(n_steps4):
+            m4.training_step(xb[i % n_batches], tb[i % n_batches], lo)
+            if i >= n_steps4 - 10:
+                losses.append(lo.clone())
+        s1.record()
+        s1.synchronize()
+        m4.sync_status()
+        ms4 = s0.elapsed_time(s1)
+        out4 = m4.inference(torch.from_numpy(x_eval).to(dev)).cpu().numpy()
+        ref4 = oracle.Oracle(henc, hnet, 10, 3).forward(x_eval, m4.get_params("inference").astype(np.float64))
+        e2e4[prec] = {"steps": n_steps4, "ms_total": ms4, "samples_per_s": n_steps4 * n4 / (ms4 * 1e-3),
+                      "final_loss": float(torch.stack(losses).mean()), "err_vs_fp64_mean_abs": float(np.abs(out4 - ref4).mean())}
+        del m4
 
     # ---- wavefront render query: 1024^2 rays, LoD pyramid 512^3 -> 4^3, 4 path vertices ----
-    from neural_lod_gb300.lod import LodGrid
     from neural_lod_gb300.render import RenderParams, Renderer, camera
 
-    occ = W.value_noise_occupancy(256, seed=5, spacing=16, density=0.3)
-    occ = occ.repeat(2, 0).repeat(2, 1).repeat(2, 2)
+    occ = noise256.repeat(2, 0).repeat(2, 1).repeat(2, 2)
     pyr = LodGrid(W.pack_bits(occ), 512, 8)
     del occ
     rlevel = 3
@@ -444,6 +483,9 @@ def main():
                    "cpu_sample": "96x96 rays of the same camera, FP64 host restatement, all host threads"},
         "voxelize": {"triangles": 2_000_000, "grid": 1024, "ms": tvox, "triangles_per_s": 2e6 / (tvox * 1e-3),
                      "scene": "20k ellipsoid shells (48 tris) + 0.52M quads, unit cube, 1e-4 padding"},
+        "voxelize_train": {"pyramid_ms": t_pyr * 1e3, "batch": n4, "batches": n_batches, **e2e4,
+                           "targets": "albedo(voxel centre) x exact-DDA transmittance along wi, LoD 0-7 of the 1024^3 pyramid",
+                           "loss": "RelativeL2", "optimizer": "Ema(0.95) of ExponentialDecay(Adam lr 5e-3)"},
         "clocks": clocks,
         "gpu_launches": len(times16),
         "kernel_variant": variant,
