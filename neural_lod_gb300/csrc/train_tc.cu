@@ -49,6 +49,8 @@ constexpr bool kScatterAggregate = false;        // one atomic per corner (see g
 
 __host__ __device__ inline uint32_t al(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
 
+constexpr uint32_t kMmaSeqBytes = 40;   // sizeof(MmaSeq)
+
 struct TrainLayout {
     uint32_t grp_base;       // first group region (after the weights)
     uint32_t h_rel;          // H[1] within a group region (X0 at 0)
@@ -57,6 +59,7 @@ struct TrainLayout {
     uint32_t lvl_off;
     uint32_t bar_off;        // ready[G], done[G], fin, xbar[G], then the TMEM slot and the abort flag
     uint32_t red_off;        // per-warp loss sums
+    uint32_t seq_off;        // MMA runs: [G][2L jobs][2]
     uint32_t total;
     uint32_t work_col, work_stride, tmem_cols;   // TMEM: dW columns of every layer, then G work regions
 };
@@ -84,6 +87,8 @@ __host__ __device__ inline TrainLayout train_layout(const ModelDesc& d, int G) {
     off += 8u * (3u * G + 1u) + 8u;
     L.red_off = al(off, 16);
     off = L.red_off + 4u * (4u * G + 1u);
+    L.seq_off = al(off, 16);
+    off = L.seq_off + (uint32_t)G * 2u * d.n_layers * 2u * kMmaSeqBytes;
     L.total = al(off, 128);
     uint32_t col = dw_col(d, d.n_layers);
     L.work_col = col;
@@ -141,10 +146,20 @@ __device__ __forceinline__ float hi16(uint32_t w) { return lo16<T>(w >> 16); }
 
 __device__ __forceinline__ uint64_t desc(uint32_t addr, uint32_t lbo, uint32_t sbo) { return tc::make_smem_desc(addr, lbo, sbo); }
 
-// Issues MMA job j of group g (forward layers 0..L-1, then backward layers L-1..0).
+// One run of dependent MMAs: count instructions whose operand descriptors advance by a_step /
+// b_step (16-byte units) per instruction.  Built once per CTA so that issuing a job is a short
+// loop of descriptor additions.
+struct MmaSeq {
+    uint64_t a, b;        // operand descriptors of the first MMA
+    uint32_t d, idesc;    // accumulator (TMEM address) and instruction descriptor
+    uint32_t a_step, b_step;
+    uint32_t count;
+    int32_t dw_layer;     // >= 0: weight-gradient run of that layer (accumulates across tiles)
+};
+
+// The MMA runs of job j of group g (forward layers 0..L-1, then backward layers L-1..0).
 template <typename T>
-__device__ __forceinline__ void issue_job(const ModelDesc& d, const TrainLayout& L, uint8_t* smem, uint32_t tmem, uint32_t g, uint32_t j,
-                                          uint32_t& dw_started) {
+__device__ void build_job(const ModelDesc& d, const TrainLayout& L, uint8_t* smem, uint32_t tmem, uint32_t g, uint32_t j, MmaSeq (&q)[2]) {
     using Op = tc::OpType<T>;
     const uint32_t nl = d.n_layers;
     const uint32_t grp = tc::smem_addr(smem + L.grp_base + g * L.group_stride);
@@ -152,13 +167,14 @@ __device__ __forceinline__ void issue_job(const ModelDesc& d, const TrainLayout&
     auto hbuf = [&](uint32_t i) { return grp + L.h_rel + (i - 1u) * kHBytes; };   // H[i], i >= 1
     const uint32_t work = tmem + L.work_col + g * L.work_stride;
     const uint32_t K0 = d.enc_width;
+    q[0].count = q[1].count = 0;
+    q[0].dw_layer = q[1].dw_layer = -1;
     if (j < nl) {
         const uint32_t f = j, K = d.layer_in[f], N = d.layer_out[f];
         const uint32_t a = f == 0 ? x0 : hbuf(f);
         const uint32_t b = tc::smem_addr(smem + 2u * d.layer_offset[f]);
-        const uint32_t idesc = tc::make_idesc_f16(Op::kFmt, 128, N);
-        for (uint32_t k = 0; k < K; k += 16)
-            tc::mma_f16_ss(work, desc(a + k * 16u, 128u, K * 16u), desc(b + k * 16u, 128u, K * 16u), idesc, k > 0 ? 1u : 0u);
+        // K-major operands: 16 more K columns = two core matrices = 256 bytes
+        q[0] = MmaSeq{desc(a, 128u, K * 16u), desc(b, 128u, K * 16u), work, tc::make_idesc_f16(Op::kFmt, 128, N), 16u, 16u, K / 16u, -1};
         return;
     }
     const uint32_t b = 2u * nl - 1u - j;
@@ -169,31 +185,41 @@ __device__ __forceinline__ void issue_job(const ModelDesc& d, const TrainLayout&
     // delta propagation: dL/d(input of layer b) = delta_b W_b  (B = W_b read MN-major)
     if (b > 0 || d.n_grids > 0) {
         const uint32_t w = tc::smem_addr(smem + 2u * d.layer_offset[b]);
-        const uint32_t idesc = tc::make_idesc_f16(Op::kFmt, 128, in_b) | tc::kIdescBMajorMN;
-        for (uint32_t k = 0; k < out_b; k += 16)
-            tc::mma_f16_ss(work, desc(delta + k * 16u, 128u, delta_ld), desc(w + (k / 8u) * (in_b * 16u), in_b * 16u, 128u), idesc,
-                           k > 0 ? 1u : 0u);
+        q[0] = MmaSeq{desc(delta, 128u, delta_ld), desc(w, in_b * 16u, 128u), work,
+                      tc::make_idesc_f16(Op::kFmt, 128, in_b) | tc::kIdescBMajorMN, 16u, (2u * in_b * 16u) >> 4, out_b / 16u, -1};
     }
     // weight gradient over the tile's rows (both operands MN-major, K = rows)
     const uint32_t dw = tmem + dw_col(d, b);
-    const bool started = (dw_started >> b) & 1u;
-    dw_started |= 1u << b;
     if (last) {
         // dW_out^T[in][out] += H[L-1]^T dz
         const uint32_t hin = nl >= 2 ? hbuf(nl - 1) : x0;
         const uint32_t hin_ld = nl >= 2 ? 64u * 16u : K0 * 16u;
-        const uint32_t idesc = tc::make_idesc_f16(Op::kFmt, 64, 16) | tc::kIdescAMajorMN | tc::kIdescBMajorMN;
-        for (uint32_t r = 0; r < kTile; r += 16)
-            tc::mma_f16_ss(dw, desc(hin + (r / 8u) * hin_ld, hin_ld, 128u), desc(dz + (r / 8u) * 256u, 256u, 128u), idesc,
-                           (started || r > 0) ? 1u : 0u);
+        q[1] = MmaSeq{desc(hin, hin_ld, 128u), desc(dz, 256u, 128u), dw,
+                      tc::make_idesc_f16(Op::kFmt, 64, 16) | tc::kIdescAMajorMN | tc::kIdescBMajorMN, (2u * hin_ld) >> 4, (2u * 256u) >> 4,
+                      kTile / 16u, (int32_t)b};
     } else {
         // dW_b[out][in] += delta_b^T A_b
         const uint32_t ain = b == 0 ? x0 : hbuf(b);
         const uint32_t ain_ld = in_b * 16u;
-        const uint32_t idesc = tc::make_idesc_f16(Op::kFmt, 64, in_b) | tc::kIdescAMajorMN | tc::kIdescBMajorMN;
-        for (uint32_t r = 0; r < kTile; r += 16)
-            tc::mma_f16_ss(dw, desc(delta + (r / 8u) * delta_ld, delta_ld, 128u), desc(ain + (r / 8u) * ain_ld, ain_ld, 128u), idesc,
-                           (started || r > 0) ? 1u : 0u);
+        q[1] = MmaSeq{desc(delta, delta_ld, 128u), desc(ain, ain_ld, 128u), dw,
+                      tc::make_idesc_f16(Op::kFmt, 64, in_b) | tc::kIdescAMajorMN | tc::kIdescBMajorMN, (2u * delta_ld) >> 4,
+                      (2u * ain_ld) >> 4, kTile / 16u, (int32_t)b};
+    }
+}
+
+static_assert(sizeof(MmaSeq) == kMmaSeqBytes, "MmaSeq layout");
+
+__device__ __forceinline__ void issue_seq(const MmaSeq& q, uint32_t& dw_started) {
+    uint32_t acc = 0;
+    if (q.dw_layer >= 0) {
+        acc = (dw_started >> q.dw_layer) & 1u;
+        dw_started |= 1u << q.dw_layer;
+    }
+    uint64_t a = q.a, b = q.b;
+    for (uint32_t k = 0; k < q.count; ++k) {
+        tc::mma_f16_ss(q.d, a, b, q.idesc, (k > 0 || acc) ? 1u : 0u);
+        a += q.a_step;
+        b += q.b_step;
     }
 }
 
@@ -269,6 +295,14 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
                 job[g] = 0;
                 if (left[g]) active |= 1u << g;
             }
+            MmaSeq* seqs = reinterpret_cast<MmaSeq*>(smem + L.seq_off);
+            for (uint32_t g = 0; g < (uint32_t)G; ++g)
+                for (uint32_t j = 0; j < 2u * nl; ++j) {
+                    MmaSeq q[2];
+                    build_job<T>(d, L, smem, tmem, g, j, q);
+                    seqs[(g * 2u * nl + j) * 2u] = q[0];
+                    seqs[(g * 2u * nl + j) * 2u + 1u] = q[1];
+                }
             long long last = clock64();
             while (active) {
                 if (*abort_flag) break;
@@ -279,7 +313,9 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
                     if (!tc::mbar_test_wait(&ready[g], (rpar >> g) & 1u)) continue;
                     rpar ^= 1u << g;
                     tc::fence_after_sync();
-                    issue_job<T>(d, L, smem, tmem, (uint32_t)g, job[g], dw_started);
+                    const MmaSeq* js = seqs + ((uint32_t)g * 2u * nl + job[g]) * 2u;
+                    issue_seq(js[0], dw_started);
+                    issue_seq(js[1], dw_started);
                     tc::mma_commit(&done[g]);
                     if (++job[g] == 2u * nl) {
                         job[g] = 0;
