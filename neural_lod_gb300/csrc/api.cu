@@ -213,6 +213,8 @@ void run_optimizer(nlod_module* m, cudaStream_t s) {
     a.loss_scale = m->grad_scale;
     a.lower_lr_bound = 0.0f;
     a.upper_lr_bound = 3.402823466e38f;
+    a.log2_beta1 = (float)std::log2((double)o.adam.beta1);
+    a.log2_beta2 = (float)std::log2((double)o.adam.beta2);
     if (o.adam.adabound) {
         a.lower_lr_bound = 0.1f - 0.1f / ((1.f - o.adam.beta2) * (float)m->step + 1.f);
         a.upper_lr_bound = 0.1f + 0.1f / ((1.f - o.adam.beta2) * (float)m->step);

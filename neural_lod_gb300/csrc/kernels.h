@@ -98,6 +98,7 @@ struct AdamStepArgs {
     float learning_rate;              // after exponential decay
     float loss_scale;
     float lower_lr_bound, upper_lr_bound;
+    float log2_beta1, log2_beta2;     // log2 of the moment decay rates (bias correction)
     float* params;                    // FP32 master
     const float* grads;               // FP32, scaled by loss_scale
     float* m1;

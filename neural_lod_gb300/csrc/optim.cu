@@ -19,32 +19,77 @@ namespace nlod {
 
 namespace {
 
-__global__ void k_adam_step(const __grid_constant__ AdamStepArgs a) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n_params) return;
+__device__ __forceinline__ float adam_one(const AdamStepArgs& a, uint32_t i, float w, float grad_scaled, float& m1, float& m2,
+                                          uint32_t& step, bool& changed) {
     const bool matrix = i < a.n_matrix;
-    float w = a.params[i];
-    float gradient = a.grads[i] / a.loss_scale;
-    bool skip = matrix ? !a.hp.optimize_matrix : (!a.hp.optimize_non_matrix || gradient == 0.f);
-    if (!skip) {
-        if (matrix) gradient += a.hp.l2_reg * w;
-        const float g2 = gradient * gradient;
-        const float m1 = a.m1[i] = a.hp.beta1 * a.m1[i] + (1.f - a.hp.beta1) * gradient;
-        const float m2 = a.m2[i] = a.hp.beta2 * a.m2[i] + (1.f - a.hp.beta2) * g2;
-        float lr = a.learning_rate;
-        if (!matrix) lr *= a.hp.non_matrix_lr_factor;
-        const uint32_t step = ++a.steps[i];
-        lr *= sqrtf(1.f - powf(a.hp.beta2, (float)step)) / (1.f - powf(a.hp.beta1, (float)step));
-        const float eff = fminf(fmaxf(lr / (sqrtf(m2) + a.hp.epsilon), a.lower_lr_bound), a.upper_lr_bound);
-        const float rel = a.hp.relative_decay * lr, absd = a.hp.absolute_decay * lr;
-        const float decayed = (1.f - rel) * w - copysignf(absd, w);
-        float nw = decayed - eff * m1;
-        if (a.hp.weight_clipping != 0.f) nw = fminf(fmaxf(nw, -a.hp.weight_clipping), a.hp.weight_clipping);
-        a.params[i] = nw;
-        w = nw;
+    float gradient = grad_scaled / a.loss_scale;
+    const bool skip = matrix ? !a.hp.optimize_matrix : (!a.hp.optimize_non_matrix || gradient == 0.f);
+    changed = !skip;
+    if (skip) return w;
+    if (matrix) gradient += a.hp.l2_reg * w;
+    const float g2 = gradient * gradient;
+    m1 = a.hp.beta1 * m1 + (1.f - a.hp.beta1) * gradient;
+    m2 = a.hp.beta2 * m2 + (1.f - a.hp.beta2) * g2;
+    float lr = a.learning_rate;
+    if (!matrix) lr *= a.hp.non_matrix_lr_factor;
+    ++step;
+    // beta^step as exp2(step * log2(beta)) (log2 of the betas computed once on the host)
+    const float b2t = exp2f((float)step * a.log2_beta2), b1t = exp2f((float)step * a.log2_beta1);
+    lr *= sqrtf(1.f - b2t) / (1.f - b1t);
+    const float eff = fminf(fmaxf(lr / (sqrtf(m2) + a.hp.epsilon), a.lower_lr_bound), a.upper_lr_bound);
+    const float rel = a.hp.relative_decay * lr, absd = a.hp.absolute_decay * lr;
+    const float decayed = (1.f - rel) * w - copysignf(absd, w);
+    float nw = decayed - eff * m1;
+    if (a.hp.weight_clipping != 0.f) nw = fminf(fmaxf(nw, -a.hp.weight_clipping), a.hp.weight_clipping);
+    return nw;
+}
+
+// Four parameters per thread with 16-byte loads and stores; moments and step counters are only
+// written for parameters that were updated.
+__global__ void __launch_bounds__(256) k_adam_step(const __grid_constant__ AdamStepArgs a) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i0 = 4u * q;
+    if (i0 >= a.n_params) return;
+    if (i0 + 4u <= a.n_params) {
+        float4 w = reinterpret_cast<const float4*>(a.params)[q];
+        const float4 g = reinterpret_cast<const float4*>(a.grads)[q];
+        float4 m1 = reinterpret_cast<const float4*>(a.m1)[q];
+        float4 m2 = reinterpret_cast<const float4*>(a.m2)[q];
+        uint4 st = reinterpret_cast<const uint4*>(a.steps)[q];
+        bool c0, c1, c2, c3;
+        w.x = adam_one(a, i0, w.x, g.x, m1.x, m2.x, st.x, c0);
+        w.y = adam_one(a, i0 + 1, w.y, g.y, m1.y, m2.y, st.y, c1);
+        w.z = adam_one(a, i0 + 2, w.z, g.z, m1.z, m2.z, st.z, c2);
+        w.w = adam_one(a, i0 + 3, w.w, g.w, m1.w, m2.w, st.w, c3);
+        if (c0 | c1 | c2 | c3) {
+            reinterpret_cast<float4*>(a.params)[q] = w;
+            reinterpret_cast<float4*>(a.m1)[q] = m1;
+            reinterpret_cast<float4*>(a.m2)[q] = m2;
+            reinterpret_cast<uint4*>(a.steps)[q] = st;
+        }
+        if (a.ema) {
+            float4 e = reinterpret_cast<const float4*>(a.ema)[q];
+            const float k0 = a.ema_decay * a.ema_debias_old, k1 = 1.f - a.ema_decay;
+            e.x = (e.x * k0 + w.x * k1) * a.ema_debias_new;
+            e.y = (e.y * k0 + w.y * k1) * a.ema_debias_new;
+            e.z = (e.z * k0 + w.z * k1) * a.ema_debias_new;
+            e.w = (e.w * k0 + w.w * k1) * a.ema_debias_new;
+            reinterpret_cast<float4*>(a.ema)[q] = e;
+        }
+        return;
     }
-    if (a.ema) {
-        a.ema[i] = (a.ema[i] * a.ema_decay * a.ema_debias_old + w * (1.f - a.ema_decay)) * a.ema_debias_new;
+    for (uint32_t i = i0; i < a.n_params; ++i) {
+        float m1 = a.m1[i], m2 = a.m2[i];
+        uint32_t st = a.steps[i];
+        bool c;
+        const float w = adam_one(a, i, a.params[i], a.grads[i], m1, m2, st, c);
+        if (c) {
+            a.params[i] = w;
+            a.m1[i] = m1;
+            a.m2[i] = m2;
+            a.steps[i] = st;
+        }
+        if (a.ema) a.ema[i] = (a.ema[i] * a.ema_decay * a.ema_debias_old + w * (1.f - a.ema_decay)) * a.ema_debias_new;
     }
 }
 
@@ -78,7 +123,8 @@ __global__ void k_init_uniform(float* __restrict__ p, uint32_t n, uint64_t seed,
 
 cudaError_t launch_adam_step(const AdamStepArgs& a, cudaStream_t s) {
     if (a.n_params == 0) return cudaSuccess;
-    k_adam_step<<<(a.n_params + 255) / 256, 256, 0, s>>>(a);
+    const uint32_t threads = (a.n_params + 3u) / 4u;
+    k_adam_step<<<(threads + 255) / 256, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
