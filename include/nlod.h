@@ -313,6 +313,28 @@ NLOD_API int nlod_render_frame(nlod_renderer* r, void* stream, float* image, uin
  * its round bound. */
 NLOD_API int nlod_render_stats(nlod_renderer* r, void* stream, uint64_t* out4);
 
+/* ---- Per-voxel visibility thresholds ----------------------------------------------------------
+ * optimise_thresholds_for_voxel_grid (rptr/cuda/neural-lod/neural_lod_learning.cu:122-293, metrics
+ * neural_lod_learning_common.cuh:836-927): for each voxel, the thresholds k/100 (k = 0..100) are
+ * scored on its samples (reference 0/1, probability p, occluded when p > t) with the chosen metric,
+ * and the middle of the run of best scores (equal within 1e-4) is kept.  Samples of voxel v are
+ * entries [v * n_samples, (v + 1) * n_samples) of truth / proba (device); thresholds: [n_voxels]
+ * device floats, the reference's optimal_thresholds/<lod>.bin contents.  Asynchronous. */
+#define NLOD_METRIC_PRECISION               0
+#define NLOD_METRIC_RECALL                  1
+#define NLOD_METRIC_FSCORE                  2
+#define NLOD_METRIC_FSCORE_MACRO            3
+#define NLOD_METRIC_FSCORE_WEIGHTED         4
+#define NLOD_METRIC_OPTIMAL_FSCORE_WEIGHTED 5   /* the reference's default */
+#define NLOD_METRIC_MCC                     6
+#define NLOD_METRIC_COHEN_KAPPA             7
+#define NLOD_METRIC_ACCURACY                8
+#define NLOD_METRIC_BALANCED_ACCURACY       9
+#define NLOD_METRIC_FOWLKES_MALLOWS         10
+#define NLOD_METRIC_YOUDEN_J                11
+NLOD_API int nlod_optimal_thresholds(const float* truth, const float* proba, uint32_t n_samples, uint32_t n_voxels, int metric,
+                                     float beta, float* thresholds, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,7 @@ SIGNATURES = [
     ("nlod_renderer_destroy", None, [_vp]),
     ("nlod_render_frame", C.c_int, [_vp, _vp, _fp, _fp]),
     ("nlod_render_stats", C.c_int, [_vp, _vp, _fp]),
+    ("nlod_optimal_thresholds", C.c_int, [_fp, _fp, _u32, _u32, C.c_int, C.c_float, _fp, _vp]),
 ]
 
 _lib = None

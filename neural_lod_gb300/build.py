@@ -46,8 +46,13 @@ def _headers_mtime() -> float:
     return max((h.stat().st_mtime for h in hs), default=0.0)
 
 
+# Units whose float expressions must not be contracted into multiply-adds (their results are
+# compared bit for bit with a host restatement).
+PER_FILE_FLAGS = {"thresholds.cu": ["-fmad=false"]}
+
+
 def _compile(src: Path, obj: Path, extra: list[str]) -> tuple[Path, str]:
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *PER_FILE_FLAGS.get(src.name, []), *extra, "-c", str(src), "-o", str(obj)]
     p = subprocess.run(cmd, capture_output=True, text=True)
     if p.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src.name}:\n{' '.join(cmd)}\n{p.stdout}\n{p.stderr}")

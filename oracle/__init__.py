@@ -74,6 +74,8 @@ def declare(L):
     L.orc_lod_level.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp, vp]
     L.orc_first_active_voxel_batch.restype = None
     L.orc_first_active_voxel_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.orc_optimal_thresholds.restype = None
+    L.orc_optimal_thresholds.argtypes = [vp, vp, C.c_uint32, C.c_uint32, ci, f32, vp]
     L.orc_render.restype = None
     L.orc_render.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.orc_mesh_frame.restype = None
@@ -264,6 +266,16 @@ def render(vis: "Oracle", vis_params, thr: "Oracle", thr_params, level: "LodLeve
     return image.reshape(params.height, params.width, 3), stats, tuple(int(v) for v in totals)
 
 
+def optimal_thresholds(truth, proba, n_samples: int, metric: int = 5, beta: float = 1.0):
+    """Per-voxel optimal visibility thresholds (the reference's threshold optimisation)."""
+    t = np.ascontiguousarray(truth, dtype=np.float32).reshape(-1)
+    p = np.ascontiguousarray(proba, dtype=np.float32).reshape(-1)
+    n_vox = t.size // n_samples
+    out = np.zeros(n_vox, np.float32)
+    lib().orc_optimal_thresholds(t.ctypes.data, p.ctypes.data, n_samples, n_vox, metric, C.c_float(beta), out.ctypes.data)
+    return out
+
+
 def mesh_frame(mesh_min, mesh_max, grid: int, eps: float = 1e-4):
     """createMeshBBCube + voxinfo: (bbox_min, bbox_max, unit), each float32[3]."""
     mn = np.ascontiguousarray(mesh_min, dtype=np.float32)
@@ -291,4 +303,4 @@ def sh(degree: int, x: float, y: float, z: float):
     return np.array(out[:], dtype=np.float64)
 
 
-__all__ = ["Oracle", "LodLevel", "adam_step", "sh", "grid_levels", "model_spec", "mesh_frame", "voxelize", "render"]
+__all__ = ["Oracle", "LodLevel", "adam_step", "sh", "grid_levels", "model_spec", "mesh_frame", "voxelize", "render", "optimal_thresholds"]

@@ -890,3 +890,83 @@ void orc_render(const OrcModel* vis, const double* vis_params, const OrcModel* t
     }
     if (totals) { totals[0] = tv; totals[1] = tt; totals[2] = dropped; }
 }
+
+/* ---------------------------------------------------------------------------------------------
+ * Per-voxel threshold optimisation (rptr/cuda/neural-lod/neural_lod_learning.cu:122-293,
+ * metrics neural_lod_learning_common.cuh:836-927), float arithmetic without contraction.
+ * ------------------------------------------------------------------------------------------- */
+static float orc_prec(uint32_t fp, uint32_t tp) { return tp == 0 ? 0.f : (float)tp / (float)(tp + fp); }
+static float orc_rec(uint32_t fn, uint32_t tp) { return tp == 0 ? 0.f : (float)tp / (float)(tp + fn); }
+static float orc_fscore(uint32_t tn, uint32_t fp, uint32_t fn, uint32_t tp, float beta) {
+    const float p = orc_prec(fp, tp), r = orc_rec(fn, tp);
+    (void)tn;
+    if (p + r == 0.f) return 0.f;
+    const float b2 = beta * beta;
+    return ((1.f + b2) * p * r) / (b2 * p + r);
+}
+
+static float orc_score(int metric, uint32_t tn, uint32_t fp, uint32_t fn, uint32_t tp, uint32_t sp, uint32_t sn, float beta) {
+    switch (metric) {
+        case 0: return orc_prec(fp, tp);
+        case 1: return orc_rec(fn, tp);
+        case 2: return orc_fscore(tn, fp, fn, tp, beta);
+        case 3: return (orc_fscore(tn, fp, fn, tp, beta) + orc_fscore(tp, fn, fp, tn, beta)) * 0.5f;
+        case 4: return (orc_fscore(tn, fp, fn, tp, beta) * sp + orc_fscore(tp, fn, fp, tn, beta) * sn) / (sp + sn);
+        case 5: return (orc_fscore(tn, fp, fn, tp, beta) * sp + orc_fscore(tp, fn, fp, tn, 1.f) * sn) / (sp + sn);
+        case 6: {
+            const float numer = (float)(tp * tn) - (float)(fp * fn);
+            const float den = (float)(tp + fp) * (float)(tp + fn) * (float)(tn + fp) * (float)(tn + fn);
+            return den == 0 ? 0.f : numer / sqrtf(den);
+        }
+        case 7: {
+            const float numer = 2.f * ((float)(tp * tn) - (float)(fn * fp));
+            const float den = (float)(tp + fp) * (float)(fp + tn) + (float)(tp + fn) * (float)(fn + tn);
+            return den == 0 ? 0.f : numer / den;
+        }
+        case 8: {
+            const float den = (float)(tp + tn + fp + fn);
+            return den == 0 ? 0.f : (float)(tp + tn) / den;
+        }
+        case 9: {
+            const float se = tp == 0 ? 0.0f : (float)tp / (float)(tp + fn), spc = tn == 0 ? 0.0f : (float)tn / (float)(tn + fp);
+            return (se + spc) * 0.5f;
+        }
+        case 10: return sqrtf(orc_prec(fp, tp) * orc_rec(fn, tp));
+        case 11: {
+            const float se = tp == 0 ? 0.0f : (float)tp / (float)(tp + fn), spc = tn == 0 ? 0.0f : (float)tn / (float)(tn + fp);
+            return se + spc - 1.f;
+        }
+        default: return 0.f;
+    }
+}
+
+void orc_optimal_thresholds(const float* truth, const float* proba, uint32_t n_samples, uint32_t n_voxels, int metric, float beta,
+                            float* out) {
+    enum { T = 101 };
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t v = 0; v < (int64_t)n_voxels; ++v) {
+        const float* tr = truth + v * (int64_t)n_samples;
+        const float* pr = proba + v * (int64_t)n_samples;
+        uint32_t pos = 0;
+        for (uint32_t i = 0; i < n_samples; ++i) pos += tr[i] == 1.0f;
+        float sc[T];
+        for (int k = 0; k < T; ++k) {
+            const float th = k / (float)(T - 1);
+            uint32_t tn = 0, fp = 0, fn = 0, tp = 0;
+            for (uint32_t i = 0; i < n_samples; ++i) {
+                const int pred = pr[i] > th, t = tr[i] == 1.0f;
+                if (!t) { if (pred) ++fp; else ++tn; }
+                else { if (pred) ++tp; else ++fn; }
+            }
+            sc[k] = orc_score(metric, tn, fp, fn, tp, pos, n_samples - pos, beta);
+        }
+        float best = -10.0f;
+        int opt = 0;
+        for (int k = 0; k < T; ++k)
+            if (sc[k] > best) { best = sc[k]; opt = k; }
+        int eq = 0;
+        while (opt + eq < T && fabsf(sc[opt + eq] - sc[opt]) < 1e-4f) ++eq;
+        opt += eq / 2;
+        out[v] = opt / (float)(T - 1);
+    }
+}

@@ -161,6 +161,10 @@ typedef struct {
 void orc_render(const OrcModel* vis, const double* vis_params, const OrcModel* thr, const double* thr_params, const OrcLodLevel* L,
                 const OrcRenderParams* p, const float cam[12], float* image, uint32_t* ray_stats, uint64_t* totals);
 
+/* Optimal per-voxel visibility thresholds (metric ids as NLOD_METRIC_* in include/nlod.h). */
+void orc_optimal_thresholds(const float* truth, const float* proba, uint32_t n_samples, uint32_t n_voxels, int metric, float beta,
+                            float* out);
+
 /* FP32 scalar forward over all host threads: the timed CPU baseline. Returns threads used. */
 int orc_forward_f32(const OrcModel* m, int64_t n, const float* in, const float* params, const float* max_level,
                     float max_level_scalar, float* out, int n_threads);
