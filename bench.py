@@ -225,7 +225,7 @@ def main():
 
     __graft_entry__.build()
     import oracle
-    from neural_lod_gb300 import NetworkWithInputEncoding, workloads as W
+    from neural_lod_gb300 import NetworkWithInputEncoding, layout, workloads as W
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -239,7 +239,7 @@ def main():
     # ---- headline: throughput query forward, batch 2^21 ----
     n = W.WORKLOADS["throughput_query"]["batch"]
     enc, net = W.throughput_configs()
-    spec = oracle.model_spec(enc, net, 10, 3)
+    spec = layout(enc, net, 10, 3)
     params = W.xavier_params(spec, seed=7 + rank)
     x_host = W.throughput_inputs(n, seed=1 + rank)
     x = torch.from_numpy(x_host).to(dev)
@@ -292,7 +292,7 @@ def main():
     # ---- visibility query, batch 65,536 ----
     nv = W.WORKLOADS["visibility_query"]["batch"]
     venc, vnet = W.visibility_configs()
-    vspec = oracle.model_spec(venc, vnet, 6, 1)
+    vspec = layout(venc, vnet, 6, 1)
     vparams = W.xavier_params(vspec, seed=8)
     xv, _, frac = W.visibility_inputs(nv, seed=2)
     xvd, fracd = torch.from_numpy(xv).to(dev), torch.from_numpy(frac).to(dev)
@@ -308,7 +308,7 @@ def main():
 
     # ---- training steps: visibility (2^18, BCE) and throughput (2^20, RelativeL2, EMA/decay Adam) ----
     def train_times(enc_, net_, n_in, n_out, loss, opt, x_np, t_np, seed, precs):
-        sp = oracle.model_spec(enc_, net_, n_in, n_out)
+        sp = layout(enc_, net_, n_in, n_out)
         pr = W.xavier_params(sp, seed=seed)
         xd_, td_ = torch.from_numpy(x_np).to(dev), torch.from_numpy(t_np).to(dev)
         res = {}
@@ -400,8 +400,8 @@ def main():
                            lod_max_level=(7 - rlevel) / 8, lod_input=(rlevel + 0.5) / 8, seed=42)
     venc, vnet = W.visibility_configs()
     henc, hnet = W.throughput_configs()
-    rv_params = W.xavier_params(oracle.model_spec(venc, vnet, 6, 1), seed=12)
-    rt_params = W.xavier_params(oracle.model_spec(henc, hnet, 10, 3), seed=13)
+    rv_params = W.xavier_params(layout(venc, vnet, 6, 1), seed=12)
+    rt_params = W.xavier_params(layout(henc, hnet, 10, 3), seed=13)
     render = {}
     for prec in ("fp16", "fp32"):
         rv = NetworkWithInputEncoding(6, 1, venc, vnet, precision=prec)

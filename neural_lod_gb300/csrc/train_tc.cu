@@ -278,8 +278,12 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t first_tile = blockIdx.x * G;
-    const uint32_t stride = gridDim.x * G;
+    // The CTA's tiles are one contiguous range (13 or 14 of 2048 tiles over 152 CTAs, where a
+    // round-robin over all groups would give 16 to some CTAs and 12 to the rest); its groups take
+    // every G-th tile of it.
+    const uint32_t first_tile = (uint32_t)(((uint64_t)blockIdx.x * n_tiles) / gridDim.x);
+    const uint32_t end_tile = (uint32_t)(((uint64_t)(blockIdx.x + 1u) * n_tiles) / gridDim.x);
+    constexpr uint32_t stride = G;
     bool aborted = false;
     float loss_acc = 0.f;
 
@@ -291,7 +295,7 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
 #pragma unroll
             for (int g = 0; g < G; ++g) {
                 const uint32_t t0 = first_tile + g;
-                left[g] = t0 < n_tiles ? (n_tiles - t0 + stride - 1) / stride : 0u;
+                left[g] = t0 < end_tile ? (end_tile - t0 + stride - 1) / stride : 0u;
                 job[g] = 0;
                 if (left[g]) active |= 1u << g;
             }
@@ -351,13 +355,13 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
         bool x_pending = false;   // a bulk copy of X0 is in flight (thread gtid 0)
         const uint32_t x0_bytes = kTile * d.enc_width * 2u;
         const uint8_t* enc_tiles = reinterpret_cast<const uint8_t*>(a.enc_tiles);
-        if (gtid == 0 && first_tile + grp_i < n_tiles) {
+        if (gtid == 0 && first_tile + grp_i < end_tile) {
             tc::mbar_arrive_expect_tx(&xbar[grp_i], x0_bytes);
             tc::bulk_copy_g2s(x0, enc_tiles + (size_t)(first_tile + grp_i) * x0_bytes, x0_bytes, &xbar[grp_i]);
             x_pending = true;
         }
 
-        for (uint32_t tile = first_tile + grp_i; tile < n_tiles; tile += stride) {
+        for (uint32_t tile = first_tile + grp_i; tile < end_tile; tile += stride) {
             const uint32_t row0 = tile * kTile;
             {
                 // X0 was encoded by k_encode_tiles; its copy was issued when the previous tile's
@@ -426,7 +430,7 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
                     }
                 } else {
                     const uint32_t b = 2u * nl - 1u - j;
-                    if (b == 0 && gtid == 0 && tile + stride < n_tiles) {
+                    if (b == 0 && gtid == 0 && tile + stride < end_tile) {
                         // every MMA reading X0 has completed: fetch the next tile during this epilogue
                         tc::mbar_arrive_expect_tx(&xbar[grp_i], x0_bytes);
                         tc::bulk_copy_g2s(x0, enc_tiles + (size_t)(tile + stride) * x0_bytes, x0_bytes, &xbar[grp_i]);
@@ -503,7 +507,7 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const bool any_tile = first_tile < n_tiles;
+    const bool any_tile = first_tile < end_tile;
     if (!*abort_flag && any_tile && warp < (uint32_t)G * 4u) {
         const uint32_t grp_i = warp >> 2, quarter = warp & 3u;
         const uint32_t m = quarter * 16u + lane;   // accumulator row (M = 64 layout)

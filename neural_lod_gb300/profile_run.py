@@ -70,10 +70,8 @@ def main():
         henc, hnet = W.throughput_configs()
         rv = N.NetworkWithInputEncoding(6, 1, venc, vnet, precision=a.precision)
         rt = N.NetworkWithInputEncoding(10, 3, henc, hnet, precision=a.precision)
-        import oracle
-
-        rv.set_params(W.xavier_params(oracle.model_spec(venc, vnet, 6, 1), seed=12))
-        rt.set_params(W.xavier_params(oracle.model_spec(henc, hnet, 10, 3), seed=13))
+        rv.set_params(W.xavier_params(N.layout(venc, vnet, 6, 1), seed=12))
+        rt.set_params(W.xavier_params(N.layout(henc, hnet, 10, 3), seed=13))
         p = RenderParams(width=1024, height=1024, level=3, lod_max_level=4 / 8, lod_input=3.5 / 8, seed=42)
         r = Renderer(rv, rt, pyr, p)
         for _ in range(a.iters):
