@@ -140,6 +140,8 @@ struct TrainTcArgs {
     float* loss_partial;              // [gridDim.x] per-CTA loss sums (nullable)
     void* enc_tiles;                  // [n/128][128 x enc_width] operand-type X0 tiles written by
                                       // launch_encode_tiles and bulk-copied by the fused kernel
+    uint32_t group_levels;            // grid levels a tile pipeline scatters itself when a
+                                      // scatter team takes the rest (set by launch_train_tc)
 };
 // Tile pipelines per CTA that fit the network (0 = network not supported by the fused kernel).
 int train_tc_groups(const ModelDesc& d);

@@ -139,11 +139,12 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
 
     for (uint32_t tile = blockIdx.x * G + grp; tile < n_tiles; tile += gridDim.x * G) {
         const uint32_t row0 = tile * kTcTile;
-        // 1. stage inputs
+        // 1. stage inputs (read once: streaming loads, so that they do not evict the grid tables
+        //    from L2)
         const float* in_tile = a.in + (size_t)row0 * d.n_input;
         for (uint32_t idx = gtid; idx < kTcTile * d.n_input; idx += kGroupThreads) {
             const uint32_t r = idx / d.n_input, c = idx - r * d.n_input;
-            in_s[r * L.in_ld + c] = __ldg(in_tile + idx);
+            in_s[r * L.in_ld + c] = __ldcs(in_tile + idx);
         }
         group_sync(bar_id);
         // 2. encoding into the A operand (K = enc_width)
@@ -204,15 +205,16 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
                 tc::tmem_wait_ld();
                 const size_t grow = (size_t)row0 + row;
                 if (a.out) {
+                    // written once: streaming stores (evict-first in L2)
                     for (uint32_t c = 0; c < d.n_output; ++c)
-                        a.out[grow * d.n_output + c] = act_fwd(d.out_act, __uint_as_float(r[c]));
+                        __stcs(a.out + grow * d.n_output + c, act_fwd(d.out_act, __uint_as_float(r[c])));
                 }
                 if (a.y) {
                     float4* yv = reinterpret_cast<float4*>(a.y + grow * 16);
 #pragma unroll
                     for (uint32_t j = 0; j < 4; ++j)
-                        yv[j] = make_float4(act_fwd(d.out_act, __uint_as_float(r[4 * j])), act_fwd(d.out_act, __uint_as_float(r[4 * j + 1])),
-                                            act_fwd(d.out_act, __uint_as_float(r[4 * j + 2])), act_fwd(d.out_act, __uint_as_float(r[4 * j + 3])));
+                        __stcs(yv + j, make_float4(act_fwd(d.out_act, __uint_as_float(r[4 * j])), act_fwd(d.out_act, __uint_as_float(r[4 * j + 1])),
+                                                   act_fwd(d.out_act, __uint_as_float(r[4 * j + 2])), act_fwd(d.out_act, __uint_as_float(r[4 * j + 3]))));
                 }
             }
             tc::fence_before_sync();

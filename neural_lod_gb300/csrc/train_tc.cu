@@ -57,7 +57,8 @@ struct TrainLayout {
     uint32_t dz_rel;
     uint32_t group_stride;
     uint32_t lvl_off;
-    uint32_t bar_off;        // ready[G], done[G], fin, xbar[G], then the TMEM slot and the abort flag
+    uint32_t bar_off;        // ready[G], done[G], fin, xbar[G], full[G], empty[G], then the TMEM
+                             // slot, the abort flag, the scatter team's pick and the hand-off tiles [G]
     uint32_t red_off;        // per-warp loss sums
     uint32_t seq_off;        // MMA runs: [G][2L jobs][2]
     uint32_t total;
@@ -84,9 +85,9 @@ __host__ __device__ inline TrainLayout train_layout(const ModelDesc& d, int G) {
     L.lvl_off = off;
     off += kMaxGrids * kMaxLevels * (uint32_t)sizeof(GridLevel);
     L.bar_off = off;
-    off += 8u * (3u * G + 1u) + 8u;
+    off += 8u * (5u * G + 1u) + 12u + 4u * G;
     L.red_off = al(off, 16);
-    off = L.red_off + 4u * (4u * G + 1u);
+    off = L.red_off + 4u * (4u * G + 5u);
     L.seq_off = al(off, 16);
     off = L.seq_off + (uint32_t)G * 2u * d.n_layers * 2u * kMmaSeqBytes;
     L.total = al(off, 128);
@@ -223,19 +224,70 @@ __device__ __forceinline__ void issue_seq(const MmaSeq& q, uint32_t& dw_started)
     }
 }
 
-template <typename T, int G>
-__global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_constant__ ModelDesc d, const __grid_constant__ TrainTcArgs a,
-                                                              uint32_t* __restrict__ status) {
+// Waits for phase `parity` of `bar`; gives up (false) when the CTA's abort flag is raised or after
+// kWaitCycles.
+__device__ __forceinline__ bool wait_unless_aborted(uint64_t* bar, uint32_t parity, volatile uint32_t* abort_flag) {
+    const long long t0 = clock64();
+    while (!tc::mbar_test_wait(bar, parity)) {
+        if (*abort_flag || clock64() - t0 > kWaitCycles) return false;
+    }
+    return true;
+}
+
+// Grid-gradient scatter of one tile row, levels [l_begin, l_end) of every grid: dL/d(grid
+// features) of the row are read from `dx` (column c of the grid features at dx[c * col_stride])
+// and reduced into the FP32 gradient tables.
+__device__ __forceinline__ void scatter_row(const ModelDesc& d, const TrainTcArgs& a, const GridLevel* lvl_s, size_t grow,
+                                            const float* dx, uint32_t col_stride, uint32_t l_begin, uint32_t l_end) {
+    uint32_t hc = 0;
+    for (uint32_t si = 0; si < d.n_slots; ++si) {
+        const Slot& s = d.slots[si];
+        if (s.type != SLOT_GRID) continue;
+        const GridDesc& gd = d.grids[s.grid];
+        const GridLevel* lv = lvl_s + s.grid * kMaxLevels;
+        const float* prow = a.in + grow * d.n_input + s.in_begin;
+        const float px = __ldg(prow), py = __ldg(prow + 1), pz = __ldg(prow + 2);
+        const float ml = a.max_level_gpu ? __ldg(a.max_level_gpu + grow) : a.max_level;
+        float* gtab = a.grads + gd.param_offset;
+        uint32_t p0, p1, p2;
+        hash_primes(gd.hash, p0, p1, p2);
+        const uint32_t le = min(l_end, gd.n_levels);
+#pragma unroll 1
+        for (uint32_t level = l_begin; level < le; ++level) {
+            const bool act = !grid_level_skipped_backward(level, ml, gd.n_levels);
+            const float2 dy = make_float2(dx[(hc + 2u * level) * col_stride] * a.grad_scale, dx[(hc + 2u * level + 1u) * col_stride] * a.grad_scale);
+            if (gd.interp == INTERP_NEAREST) grid_level_backward(gd, level, gtab, px, py, pz, dy, act);
+            else grid_level_scatter8<kScatterAggregate>(gd, lv[level], gtab, p0, p1, p2, px, py, pz, dy, act);
+        }
+        hc += 2u * gd.n_levels;
+    }
+}
+
+// ST (scatter team): most of the grid-gradient scatter runs in four extra warps.  A group that
+// finishes a tile's last backward job copies dL/d(grid features) (FP32, column-major 128 rows x
+// <= 32 columns) from TMEM into its last hidden-activation buffer, which no MMA reads until the
+// next tile's forward reaches it, hands it over (full[g]), scatters the first a.group_levels
+// levels itself and goes on with its next tile; the team scatters the other levels of the
+// hand-offs in arrival order and releases each buffer (empty[g]).  The reductions, bound by the
+// L2's reduction rate, then run continuously instead of stalling every group for the whole
+// scatter of its own tile.
+template <typename T, int G, bool ST>
+__global__ void __launch_bounds__(G * kGT + 32 + (ST ? kGT : 0), 1)
+    k_train_tc(const __grid_constant__ ModelDesc d, const __grid_constant__ TrainTcArgs a, uint32_t* __restrict__ status) {
     using Op = tc::OpType<T>;
-    constexpr uint32_t kThreads = G * kGT + 32;
+    constexpr uint32_t kThreads = G * kGT + 32 + (ST ? kGT : 0);
     extern __shared__ __align__(1024) uint8_t smem[];
     const TrainLayout L = train_layout(d, G);
     uint64_t* ready = reinterpret_cast<uint64_t*>(smem + L.bar_off);
     uint64_t* done = ready + G;
     uint64_t* fin = done + G;
     uint64_t* xbar = fin + 1;                    // X0 tile arrival (pre-encoded tiles)
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(xbar + G);
+    uint64_t* full = xbar + G;                   // hand-off of a tile's grid gradients to the team
+    uint64_t* empty = full + G;                  // the team has finished reading a hand-off
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(empty + G);
     volatile uint32_t* abort_flag = tmem_slot + 1;
+    volatile uint32_t* team_pick = tmem_slot + 2;
+    volatile uint32_t* hand_tile = tmem_slot + 3;
     float* red = reinterpret_cast<float*>(smem + L.red_off);
 
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -247,6 +299,8 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
             tc::mbar_init(&ready[g], 1);
             tc::mbar_init(&done[g], 1);
             tc::mbar_init(&xbar[g], 1);
+            tc::mbar_init(&full[g], 1);
+            tc::mbar_init(&empty[g], 1);
         }
         tc::mbar_init(fin, 1);
         *abort_flag = 0u;
@@ -339,7 +393,7 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
             if (!tc::mbar_wait_bounded(fin, 0, kWaitCycles)) atomicOr(status, 1u);
         }
         __syncwarp();
-    } else {
+    } else if (warp < (uint32_t)G * 4u) {
         // ---- tile pipeline (group) ----
         const uint32_t grp_i = warp >> 2;
         const uint32_t gtid = tid & (kGT - 1);
@@ -351,8 +405,9 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
         auto hbuf = [&](uint32_t i) { return grp + L.h_rel + (i - 1u) * kHBytes; };
         const uint32_t row = quarter * 32u + lane;
         const uint32_t taddr = tmem + L.work_col + grp_i * L.work_stride + ((quarter * 32u) << 16);
-        uint32_t dpar = 0, xpar = 0;
+        uint32_t dpar = 0, xpar = 0, epar = 0;
         bool x_pending = false;   // a bulk copy of X0 is in flight (thread gtid 0)
+        bool hand_pending = false;   // the scatter team still reads this group's last hidden buffer
         const uint32_t x0_bytes = kTile * d.enc_width * 2u;
         const uint8_t* enc_tiles = reinterpret_cast<const uint8_t*>(a.enc_tiles);
         if (gtid == 0 && first_tile + grp_i < end_tile) {
@@ -386,6 +441,16 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
                 tc::fence_after_sync();
                 const size_t grow = (size_t)row0 + row;
                 if (j + 1 < nl) {
+                    if (ST && j + 2u == nl && hand_pending) {
+                        // H[L-1] still holds the previous tile's hand-off until the team releases it
+                        const bool ok = gtid != 0 || wait_unless_aborted(&empty[grp_i], epar, abort_flag);
+                        epar ^= 1u;
+                        hand_pending = false;
+                        if (group_sync_or(bar_id, !ok)) {
+                            aborted = true;
+                            break;
+                        }
+                    }
                     // hidden layer j: activation -> H[j+1]
                     uint8_t* h = hbuf(j + 1);
 #pragma unroll
@@ -462,6 +527,33 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
                                 *p = make_uint4(ow[0], ow[1], ow[2], ow[3]);
                             }
                         }
+                    } else if (ST) {
+                        // dL/d(grid features) -> H[L-1] (column-major FP32) for the scatter team
+                        float* hand = reinterpret_cast<float*>(hbuf(nl - 1u));
+                        // (all grid levels; the group reads its own share back from here)
+                        uint32_t hc = 0;
+                        for (uint32_t si = 0; si < d.n_slots; ++si) {
+                            const Slot& s = d.slots[si];
+                            if (s.type != SLOT_GRID) continue;
+                            const uint32_t nlv = d.grids[s.grid].n_levels;
+#pragma unroll 1
+                            for (uint32_t level = 0; level < nlv; ++level) {
+                                uint32_t r0, r1;
+                                tc::tmem_ld2(taddr + s.out_begin + 2u * level, r0, r1);
+                                tc::tmem_wait_ld();
+                                hand[(hc + 2u * level) * kTile + row] = __uint_as_float(r0);
+                                hand[(hc + 2u * level + 1u) * kTile + row] = __uint_as_float(r1);
+                            }
+                            hc += 2u * nlv;
+                        }
+                        group_sync(bar_id);
+                        if (gtid == 0) {
+                            hand_tile[grp_i] = tile;
+                            tc::mbar_arrive(&full[grp_i]);
+                        }
+                        hand_pending = true;
+                        // the group's own share of the levels (the team takes the rest)
+                        scatter_row(d, a, lvl_s, grow, hand + row, kTile, 0u, a.group_levels);
                     } else if (d.n_grids > 0) {
                         // dL/dX0 -> grid-table gradients
                         for (uint32_t si = 0; si < d.n_slots; ++si) {
@@ -501,6 +593,47 @@ __global__ void __launch_bounds__(G * kGT + 32, 1) k_train_tc(const __grid_const
         }
         // a copy still in flight (only after an abort) must land before the CTA's shared memory goes
         if (x_pending) (void)tc::mbar_wait_bounded(&xbar[grp_i], xpar, kWaitCycles);
+    } else {
+        if constexpr (ST) {
+            // ---- scatter team: one thread per tile row ----
+            const uint32_t st = tid - (uint32_t)G * kGT - 32u;
+            const uint32_t team_bar = 1u + G;
+            const uint32_t total = end_tile > first_tile ? end_tile - first_tile : 0u;
+            constexpr uint32_t kNone = 0xFFFFFFFFu;
+            uint32_t fpar = 0, next = 0;
+            for (uint32_t k = 0; k < total; ++k) {
+                if (st == 0) {
+                    // the next hand-off in arrival order, groups polled round-robin
+                    uint32_t pick = kNone;
+                    const long long t0 = clock64();
+                    for (;;) {
+                        for (uint32_t i = 0; i < (uint32_t)G; ++i) {
+                            const uint32_t g = (next + i) % (uint32_t)G;
+                            if (tc::mbar_test_wait(&full[g], (fpar >> g) & 1u)) {
+                                pick = g;
+                                break;
+                            }
+                        }
+                        if (pick != kNone || *abort_flag || clock64() - t0 > kWaitCycles) break;
+                    }
+                    if (pick != kNone) {
+                        fpar ^= 1u << pick;
+                        next = (pick + 1u) % (uint32_t)G;
+                    } else {
+                        *abort_flag = 1u;
+                        atomicOr(status, 1u);
+                    }
+                    *team_pick = pick;
+                }
+                group_sync(team_bar);
+                const uint32_t pick = *team_pick;
+                if (pick == kNone) break;
+                const float* hand = reinterpret_cast<const float*>(smem + L.grp_base + pick * L.group_stride + L.h_rel + (nl - 2u) * kHBytes);
+                scatter_row(d, a, lvl_s, (size_t)hand_tile[pick] * kTile + st, hand + st, kTile, a.group_levels, kMaxLevels);
+                group_sync(team_bar);
+                if (st == 0) tc::mbar_arrive(&empty[pick]);
+            }
+        }
     }
 
     // ---- drain the weight gradients, loss partial sum ----
@@ -598,18 +731,46 @@ bool layout_ok(const ModelDesc& d, int G) {
     return L.total <= kMaxSmem && L.tmem_cols <= 512u;
 }
 
-template <typename T, int G>
-cudaError_t launch_g(const ModelDesc& d, const TrainTcArgs& a, uint32_t* status, cudaStream_t s) {
+// Grid-feature columns of the encoding (the width of a scatter-team hand-off).
+uint32_t grid_columns(const ModelDesc& d) {
+    uint32_t c = 0;
+    for (uint32_t si = 0; si < d.n_slots; ++si)
+        if (d.slots[si].type == SLOT_GRID) c += 2u * d.grids[d.slots[si].grid].n_levels;
+    return c;
+}
+
+// A hand-off (128 rows x grid columns, FP32) fits one hidden-activation buffer.
+bool use_scatter_team(const ModelDesc& d) {
+    const uint32_t c = grid_columns(d);
+    return d.n_grids > 0 && c > 0 && c * kTile * 4u <= kHBytes;
+}
+
+// Levels of every grid that a group scatters itself, the scatter team taking the rest.
+uint32_t group_scatter_levels(const ModelDesc& d, int G) {
+    uint32_t nlev = 0;
+    for (uint32_t g = 0; g < d.n_grids; ++g) nlev = d.grids[g].n_levels > nlev ? d.grids[g].n_levels : nlev;
+    return nlev / 4u;
+}
+
+template <typename T, int G, bool ST>
+cudaError_t launch_gs(const ModelDesc& d, const TrainTcArgs& a_in, uint32_t* status, cudaStream_t s) {
+    TrainTcArgs a = a_in;
+    a.group_levels = ST ? group_scatter_levels(d, G) : 0u;
     const TrainLayout L = train_layout(d, G);
     const uint32_t n_tiles = a.n / kTile;
     uint32_t blocks = (uint32_t)sm_count();
     const uint32_t need = (n_tiles + G - 1) / G;
     if (blocks > need) blocks = need;
     if (blocks == 0) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_train_tc<T, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+    cudaError_t e = cudaFuncSetAttribute(k_train_tc<T, G, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
     if (e != cudaSuccess) return e;
-    k_train_tc<T, G><<<blocks, G * kGT + 32, L.total, s>>>(d, a, status);
+    k_train_tc<T, G, ST><<<blocks, G * kGT + 32 + (ST ? kGT : 0), L.total, s>>>(d, a, status);
     return cudaGetLastError();
+}
+
+template <typename T, int G>
+cudaError_t launch_g(const ModelDesc& d, const TrainTcArgs& a, uint32_t* status, cudaStream_t s) {
+    return use_scatter_team(d) ? launch_gs<T, G, true>(d, a, status, s) : launch_gs<T, G, false>(d, a, status, s);
 }
 
 template <typename T>
