@@ -268,7 +268,8 @@ __device__ __forceinline__ void scatter_row(const ModelDesc& d, const TrainTcArg
 // <= 32 columns) from TMEM into its last hidden-activation buffer, which no MMA reads until the
 // next tile's forward reaches it, hands it over (full[g]), scatters the first a.group_levels
 // levels itself and goes on with its next tile; the team scatters the other levels of the
-// hand-offs in arrival order and releases each buffer (empty[g]).  The reductions, bound by the
+// hand-offs in arrival order and releases each buffer (empty[g]).  A group's last tile is not
+// handed over: the group scatters all of it, which keeps the team's queue short at the end.  The reductions, bound by the
 // L2's reduction rate, then run continuously instead of stalling every group for the whole
 // scatter of its own tile.
 template <typename T, int G, bool ST>
@@ -547,13 +548,18 @@ __global__ void __launch_bounds__(G * kGT + 32 + (ST ? kGT : 0), 1)
                             hc += 2u * nlv;
                         }
                         group_sync(bar_id);
-                        if (gtid == 0) {
-                            hand_tile[grp_i] = tile;
-                            tc::mbar_arrive(&full[grp_i]);
+                        if (tile + stride < end_tile) {
+                            if (gtid == 0) {
+                                hand_tile[grp_i] = tile;
+                                tc::mbar_arrive(&full[grp_i]);
+                            }
+                            hand_pending = true;
+                            // the group's own share of the levels (the team takes the rest)
+                            scatter_row(d, a, lvl_s, grow, hand + row, kTile, 0u, a.group_levels);
+                        } else {
+                            // the group's last tile: nothing left to overlap, so no hand-off
+                            scatter_row(d, a, lvl_s, grow, hand + row, kTile, 0u, kMaxLevels);
                         }
-                        hand_pending = true;
-                        // the group's own share of the levels (the team takes the rest)
-                        scatter_row(d, a, lvl_s, grow, hand + row, kTile, 0u, a.group_levels);
                     } else if (d.n_grids > 0) {
                         // dL/dX0 -> grid-table gradients
                         for (uint32_t si = 0; si < d.n_slots; ++si) {
@@ -598,7 +604,9 @@ __global__ void __launch_bounds__(G * kGT + 32 + (ST ? kGT : 0), 1)
             // ---- scatter team: one thread per tile row ----
             const uint32_t st = tid - (uint32_t)G * kGT - 32u;
             const uint32_t team_bar = 1u + G;
-            const uint32_t total = end_tile > first_tile ? end_tile - first_tile : 0u;
+            // every tile but each group's last one is handed over
+            const uint32_t n_cta = end_tile > first_tile ? end_tile - first_tile : 0u;
+            const uint32_t total = n_cta > (uint32_t)G ? n_cta - (uint32_t)G : 0u;
             constexpr uint32_t kNone = 0xFFFFFFFFu;
             uint32_t fpar = 0, next = 0;
             for (uint32_t k = 0; k < total; ++k) {
@@ -745,11 +753,13 @@ bool use_scatter_team(const ModelDesc& d) {
     return d.n_grids > 0 && c > 0 && c * kTile * 4u <= kHBytes;
 }
 
-// Levels of every grid that a group scatters itself, the scatter team taking the rest.
-uint32_t group_scatter_levels(const ModelDesc& d, int G) {
+// Levels of every grid that a group scatters itself, the scatter team taking the rest: 2 of 16
+// (measured on the visibility and throughput networks; anything from 0 to 6 is within a few
+// percent, the step being bound by the L2 reduction rate).
+uint32_t group_scatter_levels(const ModelDesc& d, int) {
     uint32_t nlev = 0;
     for (uint32_t g = 0; g < d.n_grids; ++g) nlev = d.grids[g].n_levels > nlev ? d.grids[g].n_levels : nlev;
-    return nlev / 4u;
+    return nlev / 8u;
 }
 
 template <typename T, int G, bool ST>
