@@ -335,6 +335,93 @@ NLOD_API int nlod_render_stats(nlod_renderer* r, void* stream, uint64_t* out4);
 NLOD_API int nlod_optimal_thresholds(const float* truth, const float* proba, uint32_t n_samples, uint32_t n_voxels, int metric,
                                      float beta, float* thresholds, void* stream);
 
+/* ---- Training-sample generation ---------------------------------------------------------------
+ * The reference's sampler (rptr/cuda/neural-lod/neural_lod_learning_kernels.cuh:29-238, 364-569)
+ * on the GPU, with exact-DDA stand-ins for its Vulkan ray queries (rptr/vulkan/raygen.rgen:
+ * 505-730).  All buffers are device memory; all calls are asynchronous on `stream` and need no
+ * host synchronisation between them (counts stay in device memory). */
+
+/* RenderRayQuery (rptr/librender/render_params.glsl.h:165-172), same layout (48 bytes). */
+typedef struct nlod_ray_query {
+    float origin[3];
+    int32_t mode_or_data;    /* throughput: path orders (max_throughput_depth); visibility: 0 */
+    float dir[3];
+    float t_max;             /* 1e20; -1 marks a sample whose rejection loops ran out */
+    float voxel_center[3];
+    float voxel_extent;      /* edge of the query box: voxel edge * (1 + max(dilation, bound_bias)) */
+} nlod_ray_query;
+
+/* Sampler settings (NeuralLodLearning::Params, rptr/cuda/neural-lod/neural_lod_learning.h:120-214;
+ * reference defaults: dilation_outward 0.005, dilation_inward 0, min_dilation 1e-4, bound_bias 0,
+ * pdf_strength 0, pdf_shift 0, increase_boundary_density 0, n_lods 7, grid_res 512). */
+typedef struct nlod_sampler_params {
+    float aabb_min[3];           /* voxel-grid AABB in world space */
+    float aabb_max[3];
+    float voxel_size;            /* level-0 voxel edge */
+    uint32_t grid_res;           /* level-0 voxels per axis */
+    uint32_t n_lods;             /* LoDs sampled, 1..16 */
+    float dilation_outward;
+    float dilation_inward;
+    float min_dilation;
+    float bound_bias;
+    float pdf_strength;          /* shifted_square_pdf slope */
+    float pdf_shift;             /* shifted_square_pdf shift */
+    int32_t increase_boundary_density;
+    uint32_t max_attempts;       /* bound of every rejection loop (the reference's are unbounded), > 0 */
+} nlod_sampler_params;
+
+/* Sorted Morton codes (encode_morton3, 10 bits per axis) of the set voxels of a res^3 bit grid
+ * (bit x + y*res + z*res^2, most significant bit first; res a power of two <= 1024): the
+ * reference's morton_sparse_voxel_idx_mapping (neural_lod_learning_init.cu:201-294).  Writes the
+ * number of set voxels to *count (device) and the first `capacity` codes to `codes` (NULL: count
+ * only). */
+NLOD_API int nlod_morton_voxels(const uint32_t* bits, uint32_t res, uint32_t* codes, uint32_t capacity, uint32_t* count,
+                                void* stream);
+
+/* fill_ray_queries_visibility (kernels.cuh:364-569): sample i draws from the LCG stream
+ * (batch_index * n, 0, i): a level-0 voxel of `morton` (*n_voxels codes, device count) and a LoD
+ * (shifted_square_pdf), a direction wi, the dilation of the cube and a chord of it by rejection
+ * sampling, ordered into (pi, po) by cube face.  input [n][6]: pi, po normalised to the AABB;
+ * queries [n] (nullable): ray from pi towards po; lod [n] (nullable). */
+NLOD_API int nlod_sample_visibility(const nlod_sampler_params* p, const uint32_t* morton, const uint32_t* n_voxels,
+                                    uint32_t batch_index, uint32_t n, float* input, nlod_ray_query* queries, uint32_t* lod,
+                                    void* stream);
+/* The threshold-optimisation mode of the same kernel (kernels.cuh:392-413): n_samples samples for
+ * each of voxels first_voxel .. first_voxel + n_voxels - 1 of a LoD's own sorted mapping
+ * (nlod_morton_voxels of that pyramid level); sample s of voxel v is entry s + v * n_samples and
+ * draws from the stream (first_voxel + v, 0, s). */
+NLOD_API int nlod_sample_visibility_voxels(const nlod_sampler_params* p, const uint32_t* lod_morton, uint32_t first_voxel,
+                                           uint32_t n_voxels, uint32_t n_samples, uint32_t lod, float* input,
+                                           nlod_ray_query* queries, void* stream);
+/* fill_ray_queries_throughput (kernels.cuh:100-238): voxel and LoD as above, wo uniform on the
+ * sphere, the entry point of a rejection-sampled ray of direction -wo into the dilated cube.
+ * input [n][9]: voxel centre normalised to the AABB, (wo + 1) / 2, then wi (written by
+ * nlod_trace_throughput). */
+NLOD_API int nlod_sample_throughput(const nlod_sampler_params* p, const uint32_t* morton, const uint32_t* n_voxels,
+                                    uint32_t batch_index, uint32_t n, int32_t max_orders, float* input, nlod_ray_query* queries,
+                                    uint32_t* lod, void* stream);
+
+/* Visibility targets (main_visibility_optimisation, raygen.rgen:695-730, against the voxelized
+ * scene): 1 when the query ray's first occupied level-0 voxel of `g` begins inside the query box,
+ * else 0; -1 for an invalid query.  target [n]. */
+NLOD_API int nlod_trace_visibility(const nlod_lod_grid* g, const nlod_sampler_params* p, const nlod_ray_query* queries, uint32_t n,
+                                   float* target, void* stream);
+/* Throughput targets (stand-in for the path-traced ray query, raygen.rgen:505-687, and
+ * record_ray_query_results_throughput_optim, kernels.cuh:240-278): the query ray must meet an
+ * occupied level-0 voxel inside the box, else every input and target of the sample is -1 and
+ * *n_invalid (device, nullable) counts it; wi is uniform on the sphere (LCG stream
+ * (batch_index * n, 1, i)), input[6..8] = (wi + 1) / 2 and target = the voxel's albedo if the ray
+ * from the hit point along wi leaves the box without meeting another occupied voxel, else 0
+ * (log(1 + target) when log_learning).  target [n][3]. */
+NLOD_API int nlod_trace_throughput(const nlod_lod_grid* g, const nlod_sampler_params* p, const nlod_ray_query* queries, uint32_t n,
+                                   uint32_t batch_index, int log_learning, float* input, float* target, uint32_t* n_invalid,
+                                   void* stream);
+/* copy_valid_results_throughput_optim (kernels.cuh:280-318): the samples whose first target value
+ * is not -1, in index order, at most next_multiple(count, 128) - 128 of them (the reference's
+ * training-batch rule); the number kept goes to *n_valid (device). */
+NLOD_API int nlod_compact_samples(const float* input, const float* target, uint32_t n, uint32_t n_in, uint32_t n_out,
+                                  float* valid_input, float* valid_target, uint32_t* n_valid, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

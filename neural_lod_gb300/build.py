@@ -48,7 +48,7 @@ def _headers_mtime() -> float:
 
 # Units whose float expressions must not be contracted into multiply-adds (their results are
 # compared bit for bit with a host restatement).
-PER_FILE_FLAGS = {"thresholds.cu": ["-fmad=false"]}
+PER_FILE_FLAGS = {"thresholds.cu": ["-fmad=false"], "sampler.cu": ["-fmad=false"]}
 
 
 def _compile(src: Path, obj: Path, extra: list[str]) -> tuple[Path, str]:

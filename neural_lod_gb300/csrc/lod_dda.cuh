@@ -118,12 +118,13 @@ __device__ __forceinline__ bool slab(const float (&o)[3], const float (&d)[3], c
     return true;
 }
 
-// Returns 1 on a hit, 0 on a miss, -1 when the step budget ran out.
+// Returns 1 on a hit, 0 on a miss, -1 when the step budget ran out.  The search covers ray
+// parameters [t_min, t_max] (t_max = FLT_MAX: up to the grid's active bbox).
 __device__ __forceinline__ int first_active_voxel(const LodLevelDev& L, const float (&E)[3], const float (&D)[3], float t_min, const int32_t (&prev)[3],
-                                  int32_t (&out)[3], float& t_near, float& t_far, uint32_t budget) {
+                                  int32_t (&out)[3], float& t_near, float& t_far, uint32_t budget, float t_max = FLT_MAX) {
     if (L.n_active == 0) return 0;
     const float inv[3] = {__fdiv_rn(1.f, D[0]), __fdiv_rn(1.f, D[1]), __fdiv_rn(1.f, D[2])};
-    float t0 = t_min, t1 = FLT_MAX;
+    float t0 = t_min, t1 = t_max;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         float a = (float)L.bbox_min[i], b = (float)(L.bbox_max[i] + 1);

@@ -82,6 +82,23 @@ def declare(L):
     L.orc_mesh_frame.argtypes = [vp, vp, C.c_uint32, f32, vp, vp, vp]
     L.orc_voxelize.restype = None
     L.orc_voxelize.argtypes = [vp, i64, vp, vp, C.c_uint32, vp]
+    u32 = C.c_uint32
+    L.orc_morton_voxels.restype = u32
+    L.orc_morton_voxels.argtypes = [vp, u32, vp, u32]
+    L.orc_cos_sin.restype = None
+    L.orc_cos_sin.argtypes = [f32, vp, vp]
+    L.orc_sample_visibility.restype = None
+    L.orc_sample_visibility.argtypes = [vp, vp, u32, u32, u32, vp, vp, vp]
+    L.orc_sample_visibility_voxels.restype = None
+    L.orc_sample_visibility_voxels.argtypes = [vp, vp, u32, u32, u32, u32, vp, vp]
+    L.orc_sample_throughput.restype = None
+    L.orc_sample_throughput.argtypes = [vp, vp, u32, u32, u32, C.c_int32, vp, vp, vp]
+    L.orc_trace_visibility.restype = None
+    L.orc_trace_visibility.argtypes = [vp, vp, vp, u32, vp]
+    L.orc_trace_throughput.restype = u32
+    L.orc_trace_throughput.argtypes = [vp, vp, vp, u32, u32, ci, vp, vp]
+    L.orc_compact_samples.restype = u32
+    L.orc_compact_samples.argtypes = [vp, vp, u32, u32, u32, vp, vp]
     return L
 
 
@@ -304,3 +321,97 @@ def sh(degree: int, x: float, y: float, z: float):
 
 
 __all__ = ["Oracle", "LodLevel", "adam_step", "sh", "grid_levels", "model_spec", "mesh_frame", "voxelize", "render", "optimal_thresholds"]
+
+
+# ---- training-sample generator (nlod_sampler.c) ----
+
+RAY_QUERY_DTYPE = np.dtype([("origin", "<f4", (3,)), ("mode_or_data", "<i4"), ("dir", "<f4", (3,)), ("t_max", "<f4"),
+                            ("voxel_center", "<f4", (3,)), ("voxel_extent", "<f4")])
+
+
+class SamplerParams(C.Structure):
+    """OrcSamplerParams (the layout of nlod_sampler_params)."""
+    _fields_ = [("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3), ("voxel_size", C.c_float), ("grid_res", C.c_uint32),
+                ("n_lods", C.c_uint32), ("dilation_outward", C.c_float), ("dilation_inward", C.c_float),
+                ("min_dilation", C.c_float), ("bound_bias", C.c_float), ("pdf_strength", C.c_float), ("pdf_shift", C.c_float),
+                ("increase_boundary_density", C.c_int32), ("max_attempts", C.c_uint32)]
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "SamplerParams":
+        p = cls()
+        for k, v in d.items():
+            if k in ("aabb_min", "aabb_max"):
+                getattr(p, k)[:] = [float(x) for x in v]
+            else:
+                setattr(p, k, v)
+        return p
+
+
+def morton_voxels(bits, res: int):
+    """Sorted Morton codes of the set voxels (uint32 array)."""
+    b = np.ascontiguousarray(bits, dtype=np.uint32)
+    n = lib().orc_morton_voxels(b.ctypes.data, res, None, 0)
+    out = np.zeros(max(n, 1), np.uint32)
+    lib().orc_morton_voxels(b.ctypes.data, res, out.ctypes.data, n)
+    return out[:n]
+
+
+def cos_sin(phi: float):
+    c, s = C.c_float(), C.c_float()
+    lib().orc_cos_sin(C.c_float(phi), C.byref(c), C.byref(s))
+    return c.value, s.value
+
+
+def sample_visibility(params: SamplerParams, morton, batch_index: int, n: int):
+    """(input [n,6] float32, queries [n] RAY_QUERY_DTYPE, lod [n] uint32)."""
+    m = np.ascontiguousarray(morton, dtype=np.uint32)
+    x = np.zeros((n, 6), np.float32)
+    q = np.zeros(n, RAY_QUERY_DTYPE)
+    lod = np.zeros(n, np.uint32)
+    lib().orc_sample_visibility(C.byref(params), m.ctypes.data, m.size, batch_index, n, x.ctypes.data, q.ctypes.data, lod.ctypes.data)
+    return x, q, lod
+
+
+def sample_visibility_voxels(params: SamplerParams, lod_morton, first: int, n_voxels: int, n_samples: int, lod: int):
+    m = np.ascontiguousarray(lod_morton, dtype=np.uint32)
+    n = n_voxels * n_samples
+    x = np.zeros((n, 6), np.float32)
+    q = np.zeros(n, RAY_QUERY_DTYPE)
+    lib().orc_sample_visibility_voxels(C.byref(params), m.ctypes.data, first, n_voxels, n_samples, lod, x.ctypes.data, q.ctypes.data)
+    return x, q
+
+
+def sample_throughput(params: SamplerParams, morton, batch_index: int, n: int, max_orders: int = 1000):
+    m = np.ascontiguousarray(morton, dtype=np.uint32)
+    x = np.zeros((n, 9), np.float32)
+    q = np.zeros(n, RAY_QUERY_DTYPE)
+    lod = np.zeros(n, np.uint32)
+    lib().orc_sample_throughput(C.byref(params), m.ctypes.data, m.size, batch_index, n, max_orders, x.ctypes.data, q.ctypes.data,
+                                lod.ctypes.data)
+    return x, q, lod
+
+
+def trace_visibility(level0: "LodLevel", params: SamplerParams, queries):
+    q = np.ascontiguousarray(queries, dtype=RAY_QUERY_DTYPE)
+    y = np.zeros(q.size, np.float32)
+    lib().orc_trace_visibility(C.byref(level0.s), C.byref(params), q.ctypes.data, q.size, y.ctypes.data)
+    return y
+
+
+def trace_throughput(level0: "LodLevel", params: SamplerParams, queries, x, batch_index: int, log_learning: bool = False):
+    """Fills wi into x (in place) and returns (target [n,3], n_invalid)."""
+    q = np.ascontiguousarray(queries, dtype=RAY_QUERY_DTYPE)
+    assert x.dtype == np.float32 and x.flags.c_contiguous
+    y = np.zeros((q.size, 3), np.float32)
+    bad = lib().orc_trace_throughput(C.byref(level0.s), C.byref(params), q.ctypes.data, q.size, batch_index, int(log_learning),
+                                     x.ctypes.data, y.ctypes.data)
+    return y, bad
+
+
+def compact_samples(x, y):
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    xv = np.zeros_like(x)
+    yv = np.zeros_like(y)
+    k = lib().orc_compact_samples(x.ctypes.data, y.ctypes.data, x.shape[0], x.shape[1], y.shape[1], xv.ctypes.data, yv.ctypes.data)
+    return xv[:k], yv[:k]

@@ -611,10 +611,15 @@ static int orc_slab(const float o[3], const float d[3], const int32_t ijk[3], fl
 
 int orc_first_active_voxel(const OrcLodLevel* L, const float E[3], const float D[3], float t_min, const int32_t prev[3],
                            int32_t ijk_out[3], float* t_near, float* t_far) {
+    return orc_first_active_voxel_clip(L, E, D, t_min, FLT_MAX, prev, ijk_out, t_near, t_far);
+}
+
+int orc_first_active_voxel_clip(const OrcLodLevel* L, const float E[3], const float D[3], float t_min, float t_max,
+                                const int32_t prev[3], int32_t ijk_out[3], float* t_near, float* t_far) {
     if (L->n_active == 0) return 0;
     const float inv[3] = {1.f / D[0], 1.f / D[1], 1.f / D[2]};
-    /* Ray::clip against the root bbox [min, max + 1) */
-    float t0 = t_min, t1 = FLT_MAX;
+    /* Ray::clip against the root bbox [min, max + 1), within [t_min, t_max] */
+    float t0 = t_min, t1 = t_max;
     for (int i = 0; i < 3; ++i) {
         float a = (float)L->bbox_min[i], b = (float)(L->bbox_max[i] + 1);
         if (a >= b) return 0;

@@ -133,6 +133,10 @@ void orc_lod_level(const uint32_t* bits0, int32_t res0, int32_t lod, uint32_t* b
 int orc_first_active_voxel(const OrcLodLevel* level, const float eye[3], const float dir[3], float t_min,
                            const int32_t prev[3], int32_t ijk[3], float* t_near, float* t_far);
 
+/* The same search restricted to ray parameters [t_min, t_max]. */
+int orc_first_active_voxel_clip(const OrcLodLevel* level, const float eye[3], const float dir[3], float t_min, float t_max,
+                                const int32_t prev[3], int32_t ijk[3], float* t_near, float* t_far);
+
 void orc_first_active_voxel_batch(const OrcLodLevel* level, int64_t n, const float* eye, const float* dir,
                                   const float* t_min, const int32_t* prev, int32_t* hit, int32_t* ijk,
                                   float* t_near, float* t_far);
@@ -164,6 +168,46 @@ void orc_render(const OrcModel* vis, const double* vis_params, const OrcModel* t
 /* Optimal per-voxel visibility thresholds (metric ids as NLOD_METRIC_* in include/nlod.h). */
 void orc_optimal_thresholds(const float* truth, const float* proba, uint32_t n_samples, uint32_t n_voxels, int metric, float beta,
                             float* out);
+
+/* ---- Training-sample generator (nlod_sampler.c) ----
+ * Same layouts as nlod_ray_query / nlod_sampler_params in include/nlod.h. */
+typedef struct {
+    float origin[3];
+    int32_t mode_or_data;
+    float dir[3];
+    float t_max;
+    float voxel_center[3];
+    float voxel_extent;
+} OrcRayQuery;
+
+typedef struct {
+    float aabb_min[3];
+    float aabb_max[3];
+    float voxel_size;
+    uint32_t grid_res;
+    uint32_t n_lods;
+    float dilation_outward, dilation_inward, min_dilation, bound_bias;
+    float pdf_strength, pdf_shift;
+    int32_t increase_boundary_density;
+    uint32_t max_attempts;
+} OrcSamplerParams;
+
+/* Returns the number of set voxels; writes the first `capacity` Morton codes in increasing order. */
+uint32_t orc_morton_voxels(const uint32_t* bits, uint32_t res, uint32_t* codes, uint32_t capacity);
+void orc_cos_sin(float phi, float* c, float* s);
+void orc_sample_visibility(const OrcSamplerParams* p, const uint32_t* morton, uint32_t n_voxels, uint32_t batch_index, uint32_t n,
+                           float* input, OrcRayQuery* queries, uint32_t* lod);
+void orc_sample_visibility_voxels(const OrcSamplerParams* p, const uint32_t* lod_morton, uint32_t first, uint32_t n_voxels,
+                                  uint32_t n_samples, uint32_t lod, float* input, OrcRayQuery* queries);
+void orc_sample_throughput(const OrcSamplerParams* p, const uint32_t* morton, uint32_t n_voxels, uint32_t batch_index, uint32_t n,
+                           int32_t max_orders, float* input, OrcRayQuery* queries, uint32_t* lod);
+void orc_trace_visibility(const OrcLodLevel* L0, const OrcSamplerParams* p, const OrcRayQuery* queries, uint32_t n, float* target);
+/* Returns the number of invalid samples. */
+uint32_t orc_trace_throughput(const OrcLodLevel* L0, const OrcSamplerParams* p, const OrcRayQuery* queries, uint32_t n,
+                              uint32_t batch_index, int log_learning, float* input, float* target);
+/* Returns the number of samples kept. */
+uint32_t orc_compact_samples(const float* input, const float* target, uint32_t n, uint32_t n_in, uint32_t n_out, float* valid_input,
+                             float* valid_target);
 
 /* FP32 scalar forward over all host threads: the timed CPU baseline. Returns threads used. */
 int orc_forward_f32(const OrcModel* m, int64_t n, const float* in, const float* params, const float* max_level,
