@@ -430,7 +430,43 @@ def main():
     _, _, rtot = oracle.render(oracle.Oracle(venc, vnet, 6, 1), rv_params, oracle.Oracle(henc, hnet, 10, 3), rt_params,
                                oracle.LodLevel(pyr.level_bits(rlevel), 512 >> rlevel, 0), rsmall, camera(rsmall, 512 >> rlevel))
     cpu_render_s = time.perf_counter() - t0
-    del pyr
+
+    # ---- training-sample generator: the reference's samplers + exact-DDA targets on the 512^3 scene ----
+    from neural_lod_gb300.sampler import Sampler, SamplerParams
+
+    gsp = Sampler(pyr, SamplerParams(grid_res=512, n_lods=7))
+    n_gv, n_gt = 1 << 18, 1 << 20
+
+    def gen_vis():
+        xg, qg, _ = gsp.sample_visibility(5, n_gv)
+        return xg, gsp.trace_visibility(qg)
+
+    def gen_thr():
+        xg, qg, _ = gsp.sample_throughput(5, n_gt)
+        yg, _ = gsp.trace_throughput(qg, xg, 5)
+        return gsp.compact(xg, yg)
+
+    t_gv = statistics.mean(time_steps(gen_vis, max(3, args.steps // 2), 3, flush))
+    t_gt = statistics.mean(time_steps(gen_thr, max(3, args.steps // 2), 3, flush))
+    _, yv_ = gen_vis()
+    occluded = float(yv_.mean())
+    _, _, nv_ = gen_thr()
+    n_valid_thr = int(nv_.item())
+    gsp.sync_status()
+    op_ = oracle.SamplerParams.from_dict({k: (list(getattr(gsp._c, k)) if k in ("aabb_min", "aabb_max") else getattr(gsp._c, k))
+                                          for k, _ in oracle.SamplerParams._fields_})
+    m_host = gsp.morton.cpu().numpy().view(np.uint32)
+    t0 = time.perf_counter()
+    _, q_host, _ = oracle.sample_visibility(op_, m_host, 5, 1 << 14)
+    oracle.trace_visibility(oracle.LodLevel(pyr.level_bits(0), 512, 0), op_, q_host)
+    cpu_gen_s = time.perf_counter() - t0
+    generator = {"scene": "512^3 value noise (30% occupied), 7 LoDs, unit AABB, reference sampler defaults",
+                 "visibility": {"batch": n_gv, "ms": t_gv, "samples_per_s": n_gv / (t_gv * 1e-3), "occluded_fraction": occluded},
+                 "throughput": {"batch": n_gt, "ms": t_gt, "samples_per_s": n_gt / (t_gt * 1e-3),
+                                "training_batch_after_compaction": n_valid_thr},
+                 "cpu_visibility_samples_per_s": (1 << 14) / cpu_gen_s,
+                 "cpu_sample": "2^14 visibility samples + targets, host restatement, one thread"}
+    del gsp, pyr
 
     # ---- aggregate over ranks ----
     total_queries = n * world
@@ -481,6 +517,7 @@ def main():
                    "frame": "one CUDA-graph launch (rounds in a conditional while node)", **render,
                    "cpu_queries_per_s": (rtot[0] + rtot[1]) / cpu_render_s,
                    "cpu_sample": "96x96 rays of the same camera, FP64 host restatement, all host threads"},
+        "sample_generator": generator,
         "voxelize": {"triangles": 2_000_000, "grid": 1024, "ms": tvox, "triangles_per_s": 2e6 / (tvox * 1e-3),
                      "scene": "20k ellipsoid shells (48 tris) + 0.52M quads, unit cube, 1e-4 padding"},
         "voxelize_train": {"pyramid_ms": t_pyr * 1e3, "batch": n4, "batches": n_batches, **e2e4,
