@@ -51,6 +51,28 @@ def throughput_configs():
     return encoding, network
 
 
+def arcade_throughput_configs():
+    """The throughput network shipped with the reference's arcade scene
+    (neural_lod/scenes/arcade/learned_weights/arcade_world_final_512_throughput_config.json):
+    position hash grid (7 levels, base 8, scale 2, 2^19 entries) + SH degree 8 for wo and for wi ->
+    128 x 4 ReLU -> 3 linear; RelativeL2; Ema(0.95) of ExponentialDecay(0.33 every 4000 from 8000)
+    of Adam (lr 5e-3, beta 0.9/0.99, eps 1e-15, l2 1e-8).  Returns (encoding, network, loss,
+    optimizer) for a 9-input, 3-output module."""
+    encoding = {"otype": "Composite", "nested": [
+        {"otype": "HashGrid", "n_dims_to_encode": 3, "n_levels": 7, "n_features_per_level": 2, "log2_hashmap_size": 19,
+         "base_resolution": 8, "per_level_scale": 2.0, "interpolation": "Linear"},
+        {"otype": "SphericalHarmonics", "n_dims_to_encode": 3, "degree": 8},
+        {"otype": "SphericalHarmonics", "n_dims_to_encode": 3, "degree": 8},
+    ]}
+    network = {"otype": "FullyFusedMLP", "activation": "ReLU", "output_activation": "None", "n_neurons": 128, "n_hidden_layers": 4}
+    loss = {"otype": "RelativeL2"}
+    optimizer = {"otype": "Ema", "decay": 0.95, "nested": {
+        "otype": "ExponentialDecay", "decay_base": 0.33, "decay_interval": 4000, "decay_start": 8000, "nested": {
+            "otype": "Adam", "learning_rate": 5e-3, "beta1": 0.9, "beta2": 0.99, "epsilon": 1e-15, "l2_reg": 1e-8,
+            "relative_decay": 0.0, "absolute_decay": 0.0, "adabound": False}}}
+    return encoding, network, loss, optimizer
+
+
 VISIBILITY_LOSS = {"otype": "BinaryCrossEntropy"}
 VISIBILITY_OPTIMIZER = {"otype": "Adam", "learning_rate": 1e-2, "beta1": 0.9, "beta2": 0.99, "epsilon": 1e-15,
                         "l2_reg": 1e-8}
