@@ -127,6 +127,17 @@ NLOD_API int nlod_set_max_level(nlod_module* m, float max_level);
 NLOD_API int nlod_inference(nlod_module* m, void* stream, uint32_t n, const float* in, float* out);
 
 /*
+ * The same inference on a batch in host memory (no reference counterpart: the reference's batches
+ * are already on the device).  A page-locked input (cudaHostAlloc / cudaHostRegister) is read in
+ * place by the kernel over the host link (NVLink-C2C on Grace), any other host input is first
+ * copied to device memory; the output goes to a module-owned device buffer and comes back with one
+ * copy.  in: [n][n_input_dims] FP32 host; out: [n][n_output_dims] FP32 host.  Asynchronous on
+ * `stream` for page-locked buffers: out is valid after the stream synchronises.  Calls on one
+ * module share that device buffer: two of them must not overlap on different streams.
+ */
+NLOD_API int nlod_inference_host(nlod_module* m, void* stream, uint32_t n, const float* in, float* out);
+
+/*
  * Training-mode forward (training parameters), keeping what backward needs in a context.
  * Mirrors cpp::Module::forward (cpp_api.h:80).  out may be NULL.  The context is owned by
  * the caller and freed with nlod_ctx_destroy.

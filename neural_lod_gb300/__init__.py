@@ -119,6 +119,20 @@ class NetworkWithInputEncoding:
         check(self._lib.nlod_inference(self._m, _stream_ptr(stream), n, _ptr(x), _ptr(out)))
         return out
 
+    def inference_host(self, x, out=None, stream=None):
+        """Inference on a host (CPU) batch: pinned tensors are read in place by the kernel, others
+        are staged; `out` (a CPU tensor, pinned when asynchrony matters) is valid once the stream
+        has synchronised."""
+        import torch
+
+        if x.is_cuda or (out is not None and out.is_cuda):
+            raise ValueError("inference_host takes host tensors; use inference() for device tensors")
+        x = x.contiguous()
+        if out is None:
+            out = torch.empty((x.shape[0], self.n_output_dims), dtype=torch.float32, pin_memory=True)
+        check(self._lib.nlod_inference_host(self._m, _stream_ptr(stream), x.shape[0], x.data_ptr(), out.data_ptr()))
+        return out
+
     def training_step(self, x, target, loss_out=None, stream=None, run_optimizer: bool = True):
         """Returns a 1-element cuda tensor holding this step's mean loss (no host sync)."""
         import torch

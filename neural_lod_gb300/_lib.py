@@ -42,6 +42,7 @@ SIGNATURES = [
     ("nlod_set_max_level_gpu", C.c_int, [_vp, _fp]),
     ("nlod_set_max_level", C.c_int, [_vp, C.c_float]),
     ("nlod_inference", C.c_int, [_vp, _vp, _u32, _fp, _fp]),
+    ("nlod_inference_host", C.c_int, [_vp, _vp, _u32, _fp, _fp]),
     ("nlod_forward", C.c_int, [_vp, _vp, _u32, _fp, _fp, C.POINTER(_vp)]),
     ("nlod_backward", C.c_int, [_vp, _vp, _vp, _fp, _fp]),
     ("nlod_ctx_destroy", None, [_vp]),

@@ -85,6 +85,8 @@ struct nlod_module {
     float* loss_partial = nullptr;  // per-CTA loss sums of the fused training kernel
     void* enc_tiles = nullptr;      // encoded X0 tiles of the fused training step (operand type)
     size_t enc_tiles_bytes = 0;
+    uint8_t* host_io = nullptr;     // device outputs (and staged pageable inputs) of nlod_inference_host
+    size_t host_io_bytes = 0;
 
     const float* inference_params() const { return ema ? ema : params; }
     int op_kind() const { return precision == NLOD_PRECISION_FP16 ? 1 : 2; }
@@ -427,6 +429,7 @@ void nlod_module_destroy(nlod_module* m) {
     dev_free(m->status);
     dev_free(m->loss_partial);
     dev_free(m->enc_tiles);
+    dev_free(m->host_io);
     delete m;
 }
 
@@ -464,6 +467,53 @@ int nlod_inference(nlod_module* m, void* stream, uint32_t n, const float* in, fl
         a.out = out;
         if (m->precision == NLOD_PRECISION_FP32) cuda_check(launch_forward_simt(m->d, a, 0, s), "inference");
         else cuda_check(launch_forward_tc(m->d, a, m->op_kind(), m->tc_variant, m->status, s), "inference");
+    });
+}
+
+// Device address of memory the GPU can read in place: device / managed memory, or page-locked host
+// memory (mapped under unified addressing; on Grace the kernel reads it over NVLink-C2C).  NULL for
+// pageable host memory.
+static const float* device_readable(const float* p) {
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) return p;
+    if (attr.type == cudaMemoryTypeHost && attr.devicePointer) return static_cast<const float*>(attr.devicePointer);
+    return nullptr;
+}
+
+int nlod_inference_host(nlod_module* m, void* stream, uint32_t n, const float* host_in, float* host_out) {
+    return guarded([&] {
+        if (!m) throw Error(NLOD_ERR_INVALID, "module is NULL");
+        check_batch(n);
+        if (n == 0) return;
+        if (!host_in || !host_out) throw Error(NLOD_ERR_INVALID, "input and output must not be NULL");
+        cudaStream_t s = (cudaStream_t)stream;
+        const size_t in_bytes = (size_t)n * m->d.n_input * sizeof(float);
+        const size_t out_bytes = (size_t)n * m->d.n_output * sizeof(float);
+        const size_t out_span = (out_bytes + 255) / 256 * 256;
+        const float* in_dev = device_readable(host_in);
+        const size_t need = out_span + (in_dev ? 0 : in_bytes);
+        if (m->host_io_bytes < need) {
+            dev_free(m->host_io);
+            m->host_io = nullptr;
+            m->host_io_bytes = 0;
+            m->host_io = dev_alloc<uint8_t>(need);
+            m->host_io_bytes = need;
+        }
+        float* out_dev = reinterpret_cast<float*>(m->host_io);
+        if (!in_dev) {
+            float* stage = reinterpret_cast<float*>(m->host_io + out_span);
+            cuda_check(cudaMemcpyAsync(stage, host_in, in_bytes, cudaMemcpyHostToDevice, s), "input copy");
+            in_dev = stage;
+        }
+        ForwardArgs a = base_forward_args(m, n, in_dev, true);
+        a.out = out_dev;
+        if (m->precision == NLOD_PRECISION_FP32) cuda_check(launch_forward_simt(m->d, a, 0, s), "inference");
+        else cuda_check(launch_forward_tc(m->d, a, m->op_kind(), m->tc_variant, m->status, s), "inference");
+        cuda_check(cudaMemcpyAsync(host_out, out_dev, out_bytes, cudaMemcpyDeviceToHost, s), "output copy");
     });
 }
 

@@ -171,3 +171,23 @@ def test_deterministic(cuda, nlod_lib):
     a = m.inference(x).cpu().numpy()
     b = m.inference(x).cpu().numpy()
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", ["fp16", "fp32"])
+def test_inference_from_host_buffers(cuda, nlod_lib, precision):
+    """nlod_inference_host: a pinned input read in place, a pageable one staged; both give the
+    device call's outputs bit for bit."""
+    import torch
+
+    m, _, _ = _net(W.throughput_configs(), 10, 3, precision, grid_scale=0.2)
+    xh = torch.from_numpy(W.throughput_inputs(8192, seed=9))
+    ref = m.inference(xh.to(cuda)).cpu()
+    pinned = m.inference_host(xh.pin_memory())
+    torch.cuda.synchronize()
+    assert pinned.is_pinned() and torch.equal(pinned, ref)
+    out = torch.zeros((8192, 3), dtype=torch.float32)        # pageable output and input
+    m.inference_host(xh.clone(), out)
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref)
+    with pytest.raises(ValueError):
+        m.inference_host(xh.to(cuda))
