@@ -104,8 +104,10 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def time_steps(fn, steps, warmup, flush=None, stream=None):
-    """Per-step CUDA-event durations (ms) of fn() on the current stream, L2 flushed in between."""
+def time_steps(fn, steps, warmup, flush=None, stream=None, barrier=None):
+    """Per-step CUDA-event durations (ms) of fn() on the current stream, L2 flushed in between.
+    `barrier` (the process group's, for several ranks) brackets exactly the timed steps, each
+    side after a device synchronisation."""
     import torch
 
     for _ in range(warmup):
@@ -113,6 +115,8 @@ def time_steps(fn, steps, warmup, flush=None, stream=None):
             flush()
         fn()
     torch.cuda.synchronize()
+    if barrier is not None:
+        barrier()
     times = []
     for _ in range(steps):
         if flush is not None:
@@ -124,7 +128,18 @@ def time_steps(fn, steps, warmup, flush=None, stream=None):
         e.record()
         times.append((s, e))
     torch.cuda.synchronize()
+    if barrier is not None:
+        barrier()
     return [s.elapsed_time(e) for s, e in times]
+
+
+def max_over_ranks(values, dist_mod, device):
+    """Element-wise maximum of a list of floats over every rank of the default process group."""
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist_mod.all_reduce(t, op=dist_mod.ReduceOp.MAX)
+    return [float(v) for v in t]
 
 
 def traffic_from_profile():
@@ -267,7 +282,7 @@ def main():
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         t_wall0 = time.perf_counter()
-        times16 = time_steps(lambda: m16.inference(x, out), args.steps, args.warmup, flush)
+        times16 = time_steps(lambda: m16.inference(x, out), args.steps, args.warmup, flush, barrier=pg.barrier if pg else None)
         t_wall = time.perf_counter() - t_wall0
     clocks = clk.summary()
     torch.cuda.synchronize()
@@ -285,7 +300,7 @@ def main():
     def e2e_step():
         m16.inference_host(x_pin, out_pin)
 
-    times_e2e = time_steps(e2e_step, max(3, args.steps // 2), 3, flush)
+    times_e2e = time_steps(e2e_step, max(3, args.steps // 2), 3, flush, barrier=pg.barrier if pg else None)
     ms_e2e = statistics.mean(times_e2e)
 
     # ---- visibility query, batch 65,536 ----
@@ -471,9 +486,7 @@ def main():
     total_queries = n * world
     t_step = ms16
     if pg:
-        tt_ = torch.tensor([ms16, ms_e2e], device=dev)
-        pg.all_reduce(tt_, op=pg.ReduceOp.MAX)
-        t_step, ms_e2e = float(tt_[0]), float(tt_[1])
+        t_step, ms_e2e = max_over_ranks([ms16, ms_e2e], pg, dev)
     value = total_queries / (t_step * 1e-3)
     e2e_value = total_queries / (ms_e2e * 1e-3)
 
