@@ -103,22 +103,23 @@ __device__ inline void cos_sin(float phi, float& c_out, float& s_out) {
     const double q = floor(d * 0.63661977236758134 + 0.5);
     const double r = d - q * 1.5707963267948966;
     const double r2 = r * r;
-    double t = 1.0 - r2 / 272.0;
-    t = 1.0 - r2 / 210.0 * t;
-    t = 1.0 - r2 / 156.0 * t;
-    t = 1.0 - r2 / 110.0 * t;
-    t = 1.0 - r2 / 72.0 * t;
-    t = 1.0 - r2 / 42.0 * t;
-    t = 1.0 - r2 / 20.0 * t;
-    const double sr = r * (1.0 - r2 / 6.0 * t);
-    double u = 1.0 - r2 / 240.0;
-    u = 1.0 - r2 / 182.0 * u;
-    u = 1.0 - r2 / 132.0 * u;
-    u = 1.0 - r2 / 90.0 * u;
-    u = 1.0 - r2 / 56.0 * u;
-    u = 1.0 - r2 / 30.0 * u;
-    u = 1.0 - r2 / 12.0 * u;
-    const double cr = 1.0 - r2 / 2.0 * u;
+    // (reciprocals folded at compile time: multiplications only, FP64 division is slow here)
+    double t = 1.0 - r2 * (1.0 / 272.0);
+    t = 1.0 - r2 * (1.0 / 210.0) * t;
+    t = 1.0 - r2 * (1.0 / 156.0) * t;
+    t = 1.0 - r2 * (1.0 / 110.0) * t;
+    t = 1.0 - r2 * (1.0 / 72.0) * t;
+    t = 1.0 - r2 * (1.0 / 42.0) * t;
+    t = 1.0 - r2 * (1.0 / 20.0) * t;
+    const double sr = r * (1.0 - r2 * (1.0 / 6.0) * t);
+    double u = 1.0 - r2 * (1.0 / 240.0);
+    u = 1.0 - r2 * (1.0 / 182.0) * u;
+    u = 1.0 - r2 * (1.0 / 132.0) * u;
+    u = 1.0 - r2 * (1.0 / 90.0) * u;
+    u = 1.0 - r2 * (1.0 / 56.0) * u;
+    u = 1.0 - r2 * (1.0 / 30.0) * u;
+    u = 1.0 - r2 * (1.0 / 12.0) * u;
+    const double cr = 1.0 - r2 * 0.5 * u;
     const int m = ((int)q) & 3;
     const double c = m == 0 ? cr : m == 1 ? -sr : m == 2 ? -cr : sr;
     const double s = m == 0 ? sr : m == 1 ? cr : m == 2 ? -sr : -cr;
@@ -164,22 +165,34 @@ __device__ inline bool intersect_box0(const float (&o)[3], const float (&d)[3], 
     return true;
 }
 
-// sample_discrete_lods with shifted_square_pdf (kernels.cuh:33-70).  A sample that no
-// normalised CDF entry exceeds (sample == 1) takes the last LoD.
-__device__ inline float lod_pdf(uint32_t l, float strength, float shift, uint32_t n_lods) {
-    const float x = (float)l / (float)n_lods + shift - 0.5f + 0.0625f;
-    return (float)(1.0 + (double)(strength * x * x));
-}
-__device__ inline uint32_t sample_lod(float sample, float strength, float shift, uint32_t n_lods) {
-    // the CDF is accumulated twice (total, then the running sum) instead of stored
-    double total = 0.0;
-    for (uint32_t l = 0; l < n_lods; ++l) total = l == 0 ? (double)lod_pdf(l, strength, shift, n_lods) : total + (double)lod_pdf(l, strength, shift, n_lods);
-    double cdf = 0.0;
-    for (uint32_t l = 0; l < n_lods; ++l) {
-        cdf = l == 0 ? (double)lod_pdf(l, strength, shift, n_lods) : cdf + (double)lod_pdf(l, strength, shift, n_lods);
-        if ((double)sample < cdf / total) return l;
-    }
+// sample_discrete_lods with shifted_square_pdf (kernels.cuh:33-70): the first LoD whose
+// normalised CDF (double) exceeds the float sample; a sample no entry exceeds (sample == 1) takes
+// the last LoD.  The host turns each CDF entry c into the smallest float >= c, so that
+// `sample < c` is the float comparison `sample < bound` (LodBounds).
+struct LodBounds {
+    float b[kMaxLods];
+};
+__device__ inline uint32_t sample_lod(float sample, const LodBounds& lb, uint32_t n_lods) {
+    for (uint32_t l = 0; l < n_lods; ++l)
+        if (sample < lb.b[l]) return l;
     return n_lods - 1;
+}
+
+LodBounds lod_bounds(const nlod_sampler_params& p) {
+    double cdf[kMaxLods];
+    for (uint32_t l = 0; l < p.n_lods; ++l) {
+        const float x = (float)l / (float)p.n_lods + p.pdf_shift - 0.5f + 0.0625f;
+        const float pdf = (float)(1.0 + (double)(p.pdf_strength * x * x));
+        cdf[l] = l == 0 ? (double)pdf : cdf[l - 1] + (double)pdf;
+    }
+    LodBounds lb{};
+    for (uint32_t l = 0; l < p.n_lods; ++l) {
+        const double c = cdf[l] / cdf[p.n_lods - 1];
+        float f = (float)c;
+        if ((double)f < c) f = std::nextafter(f, INFINITY);
+        lb.b[l] = f;
+    }
+    return lb;
 }
 
 struct Voxel {
@@ -201,10 +214,11 @@ __device__ inline Voxel lod_voxel(const nlod_sampler_params& p, uint32_t x, uint
 }
 
 // sample_voxel (kernels.cuh:72-98)
-__device__ inline Voxel pick_voxel(Lcg& rng, const nlod_sampler_params& p, const uint32_t* morton, uint32_t n_voxels, uint32_t& lod) {
+__device__ inline Voxel pick_voxel(Lcg& rng, const nlod_sampler_params& p, const LodBounds& lb, const uint32_t* morton, uint32_t n_voxels,
+                                   uint32_t& lod) {
     const uint32_t sparse_idx = (uint32_t)(rng.next() * (float)n_voxels) % n_voxels;
     const uint32_t code = morton[sparse_idx];
-    lod = sample_lod(rng.next(), p.pdf_strength, p.pdf_shift, p.n_lods);
+    lod = sample_lod(rng.next(), lb, p.n_lods);
     return lod_voxel(p, compact1by2(code) >> lod, compact1by2(code >> 1) >> lod, compact1by2(code >> 2) >> lod, lod);
 }
 
@@ -340,7 +354,7 @@ __device__ void visibility_sample(Lcg& rng, const nlod_sampler_params& p, const 
     normalise_input(p, po, in + 3);
 }
 
-__global__ void __launch_bounds__(kBlock) k_sample_visibility(nlod_sampler_params p, const uint32_t* __restrict__ morton,
+__global__ void __launch_bounds__(kBlock) k_sample_visibility(nlod_sampler_params p, LodBounds lb, const uint32_t* __restrict__ morton,
                                                                const uint32_t* __restrict__ n_voxels_dev, uint32_t batch_index,
                                                                uint32_t n, float* __restrict__ input, nlod_ray_query* __restrict__ queries,
                                                                uint32_t* __restrict__ lod_out) {
@@ -354,7 +368,7 @@ __global__ void __launch_bounds__(kBlock) k_sample_visibility(nlod_sampler_param
     if (n_voxels == 0) {
         mark_invalid(in, 6, q);
     } else {
-        const Voxel vx = pick_voxel(rng, p, morton, n_voxels, lod);
+        const Voxel vx = pick_voxel(rng, p, lb, morton, n_voxels, lod);
         visibility_sample(rng, p, vx, in, q);
     }
     if (queries) queries[i] = q;
@@ -377,7 +391,7 @@ __global__ void __launch_bounds__(kBlock) k_sample_visibility_voxels(nlod_sample
     if (queries) queries[i] = q;
 }
 
-__global__ void __launch_bounds__(kBlock) k_sample_throughput(nlod_sampler_params p, const uint32_t* __restrict__ morton,
+__global__ void __launch_bounds__(kBlock) k_sample_throughput(nlod_sampler_params p, LodBounds lb, const uint32_t* __restrict__ morton,
                                                                const uint32_t* __restrict__ n_voxels_dev, uint32_t batch_index,
                                                                uint32_t n, int32_t max_orders, float* __restrict__ input,
                                                                nlod_ray_query* __restrict__ queries, uint32_t* __restrict__ lod_out) {
@@ -392,7 +406,7 @@ __global__ void __launch_bounds__(kBlock) k_sample_throughput(nlod_sampler_param
     Voxel vx{};
     float wo[3] = {0.f, 0.f, 0.f}, a[3], b[3], dil = 0.f;
     if (ok) {
-        vx = pick_voxel(rng, p, morton, n_voxels, lod);
+        vx = pick_voxel(rng, p, lb, morton, n_voxels, lod);
         const float dist = 2.f * (1.f + p.dilation_outward);
         const float u1 = rng.next();
         const float u2 = rng.next();
@@ -713,8 +727,8 @@ extern "C" int nlod_sample_visibility(const nlod_sampler_params* p, const uint32
         check_params(p);
         if (n == 0) return;
         if (!morton || !n_voxels || !input) throw Error(NLOD_ERR_INVALID, "morton, n_voxels and input must not be NULL");
-        k_sample_visibility<<<(n + kBlock - 1) / kBlock, kBlock, 0, (cudaStream_t)stream>>>(*p, morton, n_voxels, batch_index, n, input,
-                                                                                             queries, lod);
+        k_sample_visibility<<<(n + kBlock - 1) / kBlock, kBlock, 0, (cudaStream_t)stream>>>(*p, lod_bounds(*p), morton, n_voxels, batch_index,
+                                                                                             n, input, queries, lod);
         cuda_check(cudaGetLastError(), "visibility samples");
     });
 }
@@ -742,8 +756,8 @@ extern "C" int nlod_sample_throughput(const nlod_sampler_params* p, const uint32
         check_params(p);
         if (n == 0) return;
         if (!morton || !n_voxels || !input) throw Error(NLOD_ERR_INVALID, "morton, n_voxels and input must not be NULL");
-        k_sample_throughput<<<(n + kBlock - 1) / kBlock, kBlock, 0, (cudaStream_t)stream>>>(*p, morton, n_voxels, batch_index, n,
-                                                                                             max_orders, input, queries, lod);
+        k_sample_throughput<<<(n + kBlock - 1) / kBlock, kBlock, 0, (cudaStream_t)stream>>>(*p, lod_bounds(*p), morton, n_voxels,
+                                                                                             batch_index, n, max_orders, input, queries, lod);
         cuda_check(cudaGetLastError(), "throughput samples");
     });
 }

@@ -4,6 +4,7 @@
     python -m neural_lod_gb300.profile_run train  [--precision fp16] [--n 262144]  [--iters 3]
     python -m neural_lod_gb300.profile_run render [--precision fp16] [--iters 3]
     python -m neural_lod_gb300.profile_run voxelize [--iters 3]
+    python -m neural_lod_gb300.profile_run sampler  [--iters 3]
 
 `query` runs the throughput-query forward (the bench's headline kernel) `iters` times on the
 bench's inputs; `train` runs visibility training steps.  Each run ends with a status check, so a
@@ -20,7 +21,7 @@ sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["query", "train", "visq", "render", "voxelize"])
+    ap.add_argument("what", choices=["query", "train", "visq", "render", "voxelize", "sampler"])
     ap.add_argument("--precision", default="fp16")
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--iters", type=int, default=3)
@@ -79,6 +80,25 @@ def main():
         print("stats", r.stats())
         n = p.width * p.height
         m = rv
+    elif a.what == "sampler":
+        # the bench's generator workload: reference sampler defaults on the 512^3 value-noise scene,
+        # 2^18 visibility samples with targets, 2^20 throughput samples with targets and compaction
+        from neural_lod_gb300.lod import LodGrid
+        from neural_lod_gb300.sampler import Sampler, SamplerParams
+
+        occ = W.value_noise_occupancy(256, seed=5, spacing=16, density=0.3)
+        pyr = LodGrid(W.pack_bits(occ.repeat(2, 0).repeat(2, 1).repeat(2, 2)), 512, 8)
+        sp = Sampler(pyr, SamplerParams(grid_res=512, n_lods=7))
+        for it in range(a.iters):
+            xg, qg, _ = sp.sample_visibility(it, 1 << 18)
+            sp.trace_visibility(qg)
+            xt, qt, _ = sp.sample_throughput(it, 1 << 20)
+            yt, _ = sp.trace_throughput(qt, xt, it)
+            sp.compact(xt, yt)
+        sp.sync_status()
+        torch.cuda.synchronize()
+        print("ok sampler")
+        return
     elif a.what == "voxelize":
         from neural_lod_gb300 import voxelize as V
 

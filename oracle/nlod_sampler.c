@@ -88,16 +88,17 @@ static void cos_sin_f(float phi, float* c_out, float* s_out) {
     const double q = floor(d * 0.63661977236758134 + 0.5);
     const double r = d - q * 1.5707963267948966;
     const double r2 = r * r;
-    /* sin r = r (1 - r^2/(2*3) (1 - r^2/(4*5) (... (1 - r^2/(16*17))))) */
-    static const double ks[8] = {272.0, 210.0, 156.0, 110.0, 72.0, 42.0, 20.0, 6.0};
-    double t = 1.0 - r2 / ks[0];
-    for (int i = 1; i < 7; ++i) t = 1.0 - r2 / ks[i] * t;
-    const double sr = r * (1.0 - r2 / ks[7] * t);
+    /* sin r = r (1 - r^2/(2*3) (1 - r^2/(4*5) (... (1 - r^2/(16*17))))), each 1/(k(k+1)) a double
+     * constant (correctly rounded reciprocal) multiplied in */
+    static const double ks[8] = {1.0 / 272.0, 1.0 / 210.0, 1.0 / 156.0, 1.0 / 110.0, 1.0 / 72.0, 1.0 / 42.0, 1.0 / 20.0, 1.0 / 6.0};
+    double t = 1.0 - r2 * ks[0];
+    for (int i = 1; i < 7; ++i) t = 1.0 - r2 * ks[i] * t;
+    const double sr = r * (1.0 - r2 * ks[7] * t);
     /* cos r = 1 - r^2/(1*2) (1 - r^2/(3*4) (... (1 - r^2/(15*16)))) */
-    static const double kc[8] = {240.0, 182.0, 132.0, 90.0, 56.0, 30.0, 12.0, 2.0};
-    double u = 1.0 - r2 / kc[0];
-    for (int i = 1; i < 7; ++i) u = 1.0 - r2 / kc[i] * u;
-    const double cr = 1.0 - r2 / kc[7] * u;
+    static const double kc[8] = {1.0 / 240.0, 1.0 / 182.0, 1.0 / 132.0, 1.0 / 90.0, 1.0 / 56.0, 1.0 / 30.0, 1.0 / 12.0, 0.5};
+    double u = 1.0 - r2 * kc[0];
+    for (int i = 1; i < 7; ++i) u = 1.0 - r2 * kc[i] * u;
+    const double cr = 1.0 - r2 * kc[7] * u;
     switch (((int)q) & 3) {
         case 0: *c_out = (float)cr; *s_out = (float)sr; break;
         case 1: *c_out = (float)(-sr); *s_out = (float)cr; break;
