@@ -68,6 +68,7 @@ struct nlod_module {
     float* ema = nullptr;           // EMA of the parameters = inference parameters when present
     void* w_op = nullptr;           // operand copy (FP16/BF16) of the network part of `params`
     void* w_op_inf = nullptr;       // operand copy of the inference network weights
+    uint16_t* grid_h = nullptr;     // FP16 copy of the inference parameters (grid part used), FP16 modules with grids
     uint32_t* status = nullptr;     // device status word (bounded-wait timeouts)
 
     const float* max_level_gpu = nullptr;
@@ -131,6 +132,12 @@ void refresh_operand_copies(nlod_module* m, cudaStream_t s) {
     cuda_check(launch_convert_weights(m->params, m->w_op, m->d.n_params_network, m->op_kind(), s), "convert weights");
     if (m->w_op_inf != m->w_op)
         cuda_check(launch_convert_weights(m->ema, m->w_op_inf, m->d.n_params_network, m->op_kind(), s), "convert inference weights");
+    if (m->grid_h) {
+        // after every parameter change, so that captured inference (the renderer's graph) reads
+        // the current values
+        const uint32_t off = m->d.n_params_network, n = (uint32_t)(m->d.n_params - m->d.n_params_network);
+        cuda_check(launch_convert_weights(m->inference_params() + off, m->grid_h + off, n, 1, s), "convert grid tables");
+    }
 }
 
 ForwardArgs base_forward_args(nlod_module* m, uint32_t n, const float* in, bool inference) {
@@ -139,6 +146,7 @@ ForwardArgs base_forward_args(nlod_module* m, uint32_t n, const float* in, bool 
     a.in = in;
     a.params = inference ? m->inference_params() : m->params;
     a.weights_op = inference ? m->w_op_inf : m->w_op;
+    a.grid_h = inference ? m->grid_h : nullptr;
     a.max_level_gpu = m->max_level_gpu;
     a.max_level = m->max_level;
     return a;
@@ -329,6 +337,7 @@ int nlod_module_create(const char* encoding_json, const char* network_json, cons
                 m->w_op = dev_alloc<uint16_t>(m->d.n_params_network);
                 m->w_op_inf = m->ema ? dev_alloc<uint16_t>(m->d.n_params_network) : m->w_op;
             }
+            if (precision == NLOD_PRECISION_FP16 && m->d.n_grids > 0) m->grid_h = dev_alloc<uint16_t>(np);
             init_params(m.get(), seed);
             refresh_operand_copies(m.get(), 0);
             cuda_check(cudaDeviceSynchronize(), "init");
@@ -425,6 +434,7 @@ void nlod_module_destroy(nlod_module* m) {
     dev_free(m->steps);
     dev_free(m->ema);
     if (m->w_op_inf != m->w_op) dev_free(m->w_op_inf);
+    dev_free(m->grid_h);
     dev_free(m->w_op);
     dev_free(m->status);
     dev_free(m->loss_partial);

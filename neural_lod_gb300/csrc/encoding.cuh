@@ -16,6 +16,8 @@
 // consuming kernel) receives the features.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include <cstdint>
 
 #include "desc.h"
@@ -127,14 +129,33 @@ __device__ __forceinline__ void level_corner_entries(const GridLevel& L, uint32_
     }
 }
 
+// One grid entry (F = 2 features) of a table stored as FP32 pairs or as FP16 pairs (the half
+// copy the FP16 query kernels read, tiny-cuda-nn's half-precision parameters), and the 16- / 8-byte
+// load of the aligned entry pair {2m, 2m+1}.
+__device__ __forceinline__ float2 table_entry(const float* t, uint32_t e) { return __ldg(reinterpret_cast<const float2*>(t) + e); }
+__device__ __forceinline__ float2 table_entry(const __half* t, uint32_t e) {
+    const uint32_t w = __ldg(reinterpret_cast<const unsigned int*>(t) + e);
+    return __half22float2(*reinterpret_cast<const __half2*>(&w));
+}
+__device__ __forceinline__ void table_pair(const float* t, uint32_t even, float2& lo, float2& hi) {
+    const float4 q = __ldg(reinterpret_cast<const float4*>(t) + (even >> 1));
+    lo = make_float2(q.x, q.y);
+    hi = make_float2(q.z, q.w);
+}
+__device__ __forceinline__ void table_pair(const __half* t, uint32_t even, float2& lo, float2& hi) {
+    const uint2 q = __ldg(reinterpret_cast<const uint2*>(t) + (even >> 1));
+    lo = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
+    hi = __half22float2(*reinterpret_cast<const __half2*>(&q.y));
+}
+
 // Features of levels [l0, l0 + nl) (nl <= NL) of one grid for one element: f[2i], f[2i+1] are
 // the two features of level l0 + i.  All gathers of the group are issued before any is used.
-// `levels` is the grid's level table (the kernel parameter copy or a shared-memory copy).
-template <int NL>
+// `levels` is the grid's level table (the kernel parameter copy or a shared-memory copy); `table`
+// the grid's parameters (TT = float, or __half for the FP16 copy).
+template <int NL, typename TT = float>
 __device__ __forceinline__ void grid_group_forward(const GridDesc& g, const GridLevel* __restrict__ levels, uint32_t l0, uint32_t nl,
-                                                   const float* __restrict__ table, float px, float py, float pz, float ml_frac,
+                                                   const TT* __restrict__ table, float px, float py, float pz, float ml_frac,
                                                    float (&f)[2 * NL]) {
-    const float2* __restrict__ t2 = reinterpret_cast<const float2*>(table);
     uint32_t p0, p1, p2;
     hash_primes(g.hash, p0, p1, p2);
     float2 v[NL][8];
@@ -154,25 +175,26 @@ __device__ __forceinline__ void grid_group_forward(const GridDesc& g, const Grid
             w3[i][0] = interp_weight_fun(g.interp, fx);
             w3[i][1] = interp_weight_fun(g.interp, fy);
             w3[i][2] = interp_weight_fun(g.interp, fz);
-            const float2* lv = t2 + L.offset;
+            const TT* lv = table + 2u * L.offset;
             if (g.interp == INTERP_NEAREST) {
-                v[i][0] = __ldg(lv + level_entry(g.hash, L, cx, cy, cz));
+                v[i][0] = table_entry(lv, level_entry(g.hash, L, cx, cy, cz));
             } else {
                 uint32_t e[8];
                 level_corner_entries(L, p0, p1, p2, cx, cy, cz, e);
                 // x-adjacent corners whose entries form an aligned pair {2m, 2m+1} come in one
-                // 16-byte load (fewer L1 requests; the table is 16-byte aligned per level)
+                // 16-byte (8-byte for FP16) load: fewer L1 requests; every level starts on a
+                // multiple of 8 entries
 #pragma unroll
                 for (int c = 0; c < 8; c += 2) {
                     const uint32_t ea = e[c], eb = e[c + 1];
                     if ((ea ^ eb) == 1u) {
-                        const float4 q = __ldg(reinterpret_cast<const float4*>(lv + (ea & ~1u)));
-                        const float2 lo = make_float2(q.x, q.y), hi = make_float2(q.z, q.w);
+                        float2 lo, hi;
+                        table_pair(lv, ea & ~1u, lo, hi);
                         v[i][c] = (ea & 1u) ? hi : lo;
                         v[i][c + 1] = (ea & 1u) ? lo : hi;
                     } else {
-                        v[i][c] = __ldg(lv + ea);
-                        v[i][c + 1] = __ldg(lv + eb);
+                        v[i][c] = table_entry(lv, ea);
+                        v[i][c + 1] = table_entry(lv, eb);
                     }
                 }
             }
@@ -380,8 +402,8 @@ __device__ __forceinline__ void encode_slot_scalar(const Slot& s, const ModelDes
 // Row-per-thread encoding of a tile: thread t encodes rows t, t + nthreads, ...  The position and
 // max level of a row are read once; grid levels go NL at a time (NL * 8 gathers in flight) with
 // the level parameters read from `level_tables` (kMaxLevels entries per grid, shared memory).
-template <int NL, typename Store>
-__device__ __forceinline__ void encode_tile_rows(const ModelDesc& d, const GridLevel* level_tables, const float* __restrict__ params,
+template <int NL, typename Store, typename TT = float>
+__device__ __forceinline__ void encode_tile_rows(const ModelDesc& d, const GridLevel* level_tables, const TT* __restrict__ params,
                                                  const float* in_s, uint32_t in_ld, const float* __restrict__ ml_gpu, float ml_scalar,
                                                  uint32_t row0, uint32_t rows, uint32_t tid, uint32_t nthreads, Store& st) {
     for (uint32_t r = tid; r < rows; r += nthreads) {
@@ -393,13 +415,13 @@ __device__ __forceinline__ void encode_tile_rows(const ModelDesc& d, const GridL
                 const float px = row[s.in_begin], py = row[s.in_begin + 1], pz = row[s.in_begin + 2];
                 const GridDesc& g = d.grids[s.grid];
                 const uint32_t nlev = g.n_levels;
-                const float* table = params + g.param_offset;
+                const TT* table = params + g.param_offset;
                 const GridLevel* lv = level_tables + s.grid * kMaxLevels;
 #pragma unroll 1
                 for (uint32_t l0 = 0; l0 < nlev; l0 += NL) {
                     float f[2 * NL];
                     const uint32_t nl = min((uint32_t)NL, nlev - l0);
-                    grid_group_forward<NL>(g, lv, l0, nl, table, px, py, pz, ml, f);
+                    grid_group_forward<NL, TT>(g, lv, l0, nl, table, px, py, pz, ml, f);
                     st.run(r, s.out_begin + 2u * l0, f, 2u * nl);
                 }
                 if (s.n_pad) encode_slot_scalar(s, d, row, [&](uint32_t col, float v) { st.one(r, col, v); });

@@ -16,6 +16,7 @@ struct ForwardArgs {
     const float* in;                  // [n][n_input]
     const float* params;              // FP32 parameters (network then encoding)
     const void* weights_op;           // network weights in the operand type (FP16/BF16 forms)
+    const void* grid_h;               // FP16 copy of the parameters' grid tables (FP16 tensor-core inference)
     const float* max_level_gpu;       // nullable, [n]
     float max_level;                  // scalar fallback (1000 = off)
     float* out;                       // nullable, [n][n_output]

@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "desc.h"
 #include "encoding.cuh"
@@ -150,7 +151,13 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
         // 2. encoding into the A operand (K = enc_width)
         {
             TcStore<T> st{a_tile, d.enc_width * 16u};
-            encode_tile_rows<NL>(d, lvl_s, a.params, in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile, gtid, kGroupThreads, st);
+            // the FP16 form gathers from the FP16 copy of the grid tables (half the bytes per
+            // entry, tiny-cuda-nn's half-precision parameters), the BF16 form from the FP32 tables
+            if constexpr (std::is_same<T, __half>::value)
+                encode_tile_rows<NL>(d, lvl_s, static_cast<const __half*>(a.grid_h), in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile,
+                                     gtid, kGroupThreads, st);
+            else
+                encode_tile_rows<NL>(d, lvl_s, a.params, in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile, gtid, kGroupThreads, st);
         }
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
@@ -326,6 +333,7 @@ bool tc_supported(const ModelDesc& d) {
 
 cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, int variant, uint32_t* status, cudaStream_t s) {
     if (!tc_variant_ok(d, variant)) return cudaErrorInvalidValue;
+    if (kind == 1 && d.n_grids > 0 && !a.grid_h) return cudaErrorInvalidValue;   // the FP16 form reads the FP16 grid copy
     if (d.width == 64 && kind == 1) return launch_typed<64, __half>(d, a, variant, status, s);
     if (d.width == 64 && kind == 2) return launch_typed<64, __nv_bfloat16>(d, a, variant, status, s);
     if (d.width == 128 && kind == 1) return launch_typed<128, __half>(d, a, variant, status, s);
