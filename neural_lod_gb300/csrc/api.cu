@@ -127,12 +127,13 @@ void check_batch(uint32_t n) {
         throw Error(NLOD_ERR_INVALID, "batch size must be a multiple of 128 (got " + std::to_string(n) + ")");
 }
 
-void refresh_operand_copies(nlod_module* m, cudaStream_t s) {
+// grid_tables = false after an optimizer step, which writes the FP16 grid copy itself.
+void refresh_operand_copies(nlod_module* m, cudaStream_t s, bool grid_tables = true) {
     if (m->precision == NLOD_PRECISION_FP32) return;
     cuda_check(launch_convert_weights(m->params, m->w_op, m->d.n_params_network, m->op_kind(), s), "convert weights");
     if (m->w_op_inf != m->w_op)
         cuda_check(launch_convert_weights(m->ema, m->w_op_inf, m->d.n_params_network, m->op_kind(), s), "convert inference weights");
-    if (m->grid_h) {
+    if (m->grid_h && grid_tables) {
         // after every parameter change, so that captured inference (the renderer's graph) reads
         // the current values
         const uint32_t off = m->d.n_params_network, n = (uint32_t)(m->d.n_params - m->d.n_params_network);
@@ -240,8 +241,9 @@ void run_optimizer(nlod_module* m, cudaStream_t s) {
         a.ema_debias_old = 1.f - (float)std::pow(o.ema_decay, (float)(m->step - 1));
         a.ema_debias_new = 1.0f / (1.f - (float)std::pow(o.ema_decay, (float)m->step));
     }
+    a.grid_h = reinterpret_cast<__half*>(m->grid_h);
     cuda_check(launch_adam_step(a, s), "adam step");
-    refresh_operand_copies(m, s);
+    refresh_operand_copies(m, s, false);
 }
 
 void init_params(nlod_module* m, uint64_t seed) {

@@ -2,6 +2,7 @@
 // validate nothing (the C ABI validates first) and return the cudaError_t of the launch.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -108,6 +109,9 @@ struct AdamStepArgs {
     // EMA (nullable ema)
     float* ema;
     float ema_decay, ema_debias_old, ema_debias_new;
+    // nullable: FP16 copy of the inference values (the EMA when present) of the non-matrix
+    // parameters, refreshed in the same pass
+    __half* grid_h;
 };
 cudaError_t launch_adam_step(const AdamStepArgs& a, cudaStream_t s);
 

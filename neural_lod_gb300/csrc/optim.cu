@@ -67,6 +67,7 @@ __global__ void __launch_bounds__(256) k_adam_step(const __grid_constant__ AdamS
             reinterpret_cast<float4*>(a.m2)[q] = m2;
             reinterpret_cast<uint4*>(a.steps)[q] = st;
         }
+        float4 inf = w;
         if (a.ema) {
             float4 e = reinterpret_cast<const float4*>(a.ema)[q];
             const float k0 = a.ema_decay * a.ema_debias_old, k1 = 1.f - a.ema_decay;
@@ -75,6 +76,15 @@ __global__ void __launch_bounds__(256) k_adam_step(const __grid_constant__ AdamS
             e.z = (e.z * k0 + w.z * k1) * a.ema_debias_new;
             e.w = (e.w * k0 + w.w * k1) * a.ema_debias_new;
             reinterpret_cast<float4*>(a.ema)[q] = e;
+            inf = e;
+        }
+        // n_matrix is a multiple of 256: a group of four is all matrix or all grid parameters
+        if (a.grid_h && i0 >= a.n_matrix && (a.ema || c0 | c1 | c2 | c3)) {
+            const __half2 lo = __floats2half2_rn(inf.x, inf.y), hi = __floats2half2_rn(inf.z, inf.w);
+            uint2 pk;
+            pk.x = *reinterpret_cast<const uint32_t*>(&lo);
+            pk.y = *reinterpret_cast<const uint32_t*>(&hi);
+            reinterpret_cast<uint2*>(a.grid_h)[q] = pk;
         }
         return;
     }
@@ -89,7 +99,12 @@ __global__ void __launch_bounds__(256) k_adam_step(const __grid_constant__ AdamS
             a.m2[i] = m2;
             a.steps[i] = st;
         }
-        if (a.ema) a.ema[i] = (a.ema[i] * a.ema_decay * a.ema_debias_old + w * (1.f - a.ema_decay)) * a.ema_debias_new;
+        float inf = w;
+        if (a.ema) {
+            a.ema[i] = (a.ema[i] * a.ema_decay * a.ema_debias_old + w * (1.f - a.ema_decay)) * a.ema_debias_new;
+            inf = a.ema[i];
+        }
+        if (a.grid_h && i >= a.n_matrix) a.grid_h[i] = __float2half_rn(inf);
     }
 }
 

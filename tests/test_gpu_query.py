@@ -191,3 +191,28 @@ def test_inference_from_host_buffers(cuda, nlod_lib, precision):
     assert torch.equal(out, ref)
     with pytest.raises(ValueError):
         m.inference_host(xh.to(cuda))
+
+
+@pytest.mark.parametrize("with_ema", [False, True])
+def test_inference_after_training_reads_current_grid_tables(cuda, nlod_lib, with_ema):
+    """The FP16 form gathers from an FP16 copy of the grid tables that the optimizer step refreshes
+    in place: after training, inference equals a fresh module loaded with the inference
+    parameters, bit for bit."""
+    import torch
+
+    enc, net = W.throughput_configs()
+    opt = W.THROUGHPUT_OPTIMIZER if with_ema else W.THROUGHPUT_OPTIMIZER["nested"]["nested"]
+    m = NetworkWithInputEncoding(10, 3, enc, net, loss=W.THROUGHPUT_LOSS, optimizer=opt, precision="fp16")
+    spec = oracle.model_spec(enc, net, 10, 3)
+    m.set_params(W.test_params(spec, seed=4, grid_scale=0.2))
+    x = torch.from_numpy(W.throughput_inputs(4096, seed=10)).to(cuda)
+    t = torch.rand((4096, 3), device=cuda)
+    y0 = m.inference(x).clone()
+    for _ in range(3):
+        m.training_step(x, t)
+    y1 = m.inference(x)
+    m.sync_status()
+    assert not torch.equal(y0, y1)
+    fresh = NetworkWithInputEncoding(10, 3, enc, net, precision="fp16")
+    fresh.set_params(m.get_params("inference"))
+    assert torch.equal(fresh.inference(x), y1)
