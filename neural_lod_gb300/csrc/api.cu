@@ -127,13 +127,14 @@ void check_batch(uint32_t n) {
         throw Error(NLOD_ERR_INVALID, "batch size must be a multiple of 128 (got " + std::to_string(n) + ")");
 }
 
-// grid_tables = false after an optimizer step, which writes the FP16 grid copy itself.
-void refresh_operand_copies(nlod_module* m, cudaStream_t s, bool grid_tables = true) {
+// Derived copies of the parameters after they were set from outside (an optimizer step refreshes
+// them in its own pass).
+void refresh_operand_copies(nlod_module* m, cudaStream_t s) {
     if (m->precision == NLOD_PRECISION_FP32) return;
     cuda_check(launch_convert_weights(m->params, m->w_op, m->d.n_params_network, m->op_kind(), s), "convert weights");
     if (m->w_op_inf != m->w_op)
         cuda_check(launch_convert_weights(m->ema, m->w_op_inf, m->d.n_params_network, m->op_kind(), s), "convert inference weights");
-    if (m->grid_h && grid_tables) {
+    if (m->grid_h) {
         // after every parameter change, so that captured inference (the renderer's graph) reads
         // the current values
         const uint32_t off = m->d.n_params_network, n = (uint32_t)(m->d.n_params - m->d.n_params_network);
@@ -241,9 +242,12 @@ void run_optimizer(nlod_module* m, cudaStream_t s) {
         a.ema_debias_old = 1.f - (float)std::pow(o.ema_decay, (float)(m->step - 1));
         a.ema_debias_new = 1.0f / (1.f - (float)std::pow(o.ema_decay, (float)m->step));
     }
+    // the same pass refreshes every derived copy: operand-type weights and the FP16 grid tables
     a.grid_h = reinterpret_cast<__half*>(m->grid_h);
+    a.w_op = m->precision == NLOD_PRECISION_FP32 ? nullptr : m->w_op;
+    a.w_op_inf = m->precision == NLOD_PRECISION_FP32 ? nullptr : m->w_op_inf;
+    a.op_kind = m->op_kind();
     cuda_check(launch_adam_step(a, s), "adam step");
-    refresh_operand_copies(m, s, false);
 }
 
 void init_params(nlod_module* m, uint64_t seed) {
@@ -602,6 +606,8 @@ static int train_impl(nlod_module* m, void* stream, uint32_t n, const float* in,
             t.grad_scale = loss_scale * t.inv_n_total;
             t.grads = m->grads;
             t.loss_partial = m->loss_partial;
+            // the FP16 grid copy holds the inference values: the training values only without an EMA
+            t.grid_h = m->ema ? nullptr : m->grid_h;
             const size_t enc_bytes = (size_t)n * m->d.enc_width * 2u;
             if (m->enc_tiles_bytes < enc_bytes) {
                 dev_free(m->enc_tiles);

@@ -112,6 +112,11 @@ struct AdamStepArgs {
     // nullable: FP16 copy of the inference values (the EMA when present) of the non-matrix
     // parameters, refreshed in the same pass
     __half* grid_h;
+    // nullable: operand-type copies of the matrix parameters (training values, inference values),
+    // refreshed in the same pass; op_kind 1 = FP16, 2 = BF16
+    void* w_op;
+    void* w_op_inf;
+    int32_t op_kind;
 };
 cudaError_t launch_adam_step(const AdamStepArgs& a, cudaStream_t s);
 
@@ -145,6 +150,8 @@ struct TrainTcArgs {
     float* loss_partial;              // [gridDim.x] per-CTA loss sums (nullable)
     void* enc_tiles;                  // [n/128][128 x enc_width] operand-type X0 tiles written by
                                       // launch_encode_tiles and bulk-copied by the fused kernel
+    const void* grid_h;               // nullable: FP16 copy of the (training = inference) grid tables,
+                                      // read by launch_encode_tiles in the FP16 form
     uint32_t group_levels;            // grid levels a tile pipeline scatters itself when a
                                       // scatter team takes the rest (set by launch_train_tc)
 };

@@ -44,6 +44,25 @@ __device__ __forceinline__ float adam_one(const AdamStepArgs& a, uint32_t i, flo
     return nw;
 }
 
+// Operand-type (FP16 / BF16) copies of four / one matrix parameters.
+__device__ __forceinline__ void store_op4(void* dst, uint32_t q, float4 v, int kind) {
+    uint2 pk;
+    if (kind == 1) {
+        const __half2 lo = __floats2half2_rn(v.x, v.y), hi = __floats2half2_rn(v.z, v.w);
+        pk.x = *reinterpret_cast<const uint32_t*>(&lo);
+        pk.y = *reinterpret_cast<const uint32_t*>(&hi);
+    } else {
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+        pk.x = *reinterpret_cast<const uint32_t*>(&lo);
+        pk.y = *reinterpret_cast<const uint32_t*>(&hi);
+    }
+    reinterpret_cast<uint2*>(dst)[q] = pk;
+}
+__device__ __forceinline__ void store_op1(void* dst, uint32_t i, float v, int kind) {
+    if (kind == 1) reinterpret_cast<__half*>(dst)[i] = __float2half_rn(v);
+    else reinterpret_cast<__nv_bfloat16*>(dst)[i] = __float2bfloat16_rn(v);
+}
+
 // Four parameters per thread with 16-byte loads and stores; moments and step counters are only
 // written for parameters that were updated.
 __global__ void __launch_bounds__(256) k_adam_step(const __grid_constant__ AdamStepArgs a) {
@@ -67,6 +86,7 @@ __global__ void __launch_bounds__(256) k_adam_step(const __grid_constant__ AdamS
             reinterpret_cast<float4*>(a.m2)[q] = m2;
             reinterpret_cast<uint4*>(a.steps)[q] = st;
         }
+        if (a.w_op && i0 < a.n_matrix && (c0 | c1 | c2 | c3)) store_op4(a.w_op, q, w, a.op_kind);
         float4 inf = w;
         if (a.ema) {
             float4 e = reinterpret_cast<const float4*>(a.ema)[q];
@@ -79,6 +99,7 @@ __global__ void __launch_bounds__(256) k_adam_step(const __grid_constant__ AdamS
             inf = e;
         }
         // n_matrix is a multiple of 256: a group of four is all matrix or all grid parameters
+        if (a.w_op_inf && a.w_op_inf != a.w_op && i0 < a.n_matrix) store_op4(a.w_op_inf, q, inf, a.op_kind);
         if (a.grid_h && i0 >= a.n_matrix && (a.ema || c0 | c1 | c2 | c3)) {
             const __half2 lo = __floats2half2_rn(inf.x, inf.y), hi = __floats2half2_rn(inf.z, inf.w);
             uint2 pk;
@@ -105,6 +126,10 @@ __global__ void __launch_bounds__(256) k_adam_step(const __grid_constant__ AdamS
             inf = a.ema[i];
         }
         if (a.grid_h && i >= a.n_matrix) a.grid_h[i] = __float2half_rn(inf);
+        if (i < a.n_matrix) {
+            if (a.w_op && c) store_op1(a.w_op, i, w, a.op_kind);
+            if (a.w_op_inf && a.w_op_inf != a.w_op) store_op1(a.w_op_inf, i, inf, a.op_kind);
+        }
     }
 }
 

@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "desc.h"
 #include "encoding.cuh"
@@ -717,7 +718,13 @@ __global__ void __launch_bounds__(kTile) k_encode_tiles(const __grid_constant__ 
         }
         __syncthreads();
         TcStore<T> st{reinterpret_cast<uint8_t*>(a.enc_tiles) + tile * x0_bytes, d.enc_width * 16u};
-        encode_tile_rows<NL>(d, lvl_s, a.params, in_s, in_ld, a.max_level_gpu, a.max_level, row0, kTile, tid, kTile, st);
+        // FP16 form without an EMA: gather from the FP16 copy of the grid tables (the X0 operand is
+        // FP16 either way)
+        if (std::is_same<T, __half>::value && a.grid_h)
+            encode_tile_rows<NL>(d, lvl_s, static_cast<const __half*>(a.grid_h), in_s, in_ld, a.max_level_gpu, a.max_level, row0, kTile, tid,
+                                 kTile, st);
+        else
+            encode_tile_rows<NL>(d, lvl_s, a.params, in_s, in_ld, a.max_level_gpu, a.max_level, row0, kTile, tid, kTile, st);
     }
 }
 

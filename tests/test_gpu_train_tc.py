@@ -11,8 +11,9 @@ Two references:
     16-bit operands themselves (at the random-target starting point of these tests the gradient
     sums cancel heavily), not of the kernel;
   * a float64 model of the same computation with the kernel's roundings (weights, encoded
-    features, activations, output gradients and deltas rounded to FP16 / BF16, everything else
-    exact, products summed in float32): the network-weight gradients agree to about 1e-5
+    features, activations, output gradients and deltas rounded to FP16 / BF16, and in the FP16
+    form without an EMA the grid tables too, which it gathers from their FP16 copy; everything
+    else exact, products summed in float32): the network-weight gradients agree to about 1e-5
     relative, which pins the fused kernel's data flow.  The check allows 1e-2 (FP16) / 2e-2
     (BF16): a hidden pre-activation within rounding distance of zero can round to a different
     sign in a differently ordered sum, flipping one ReLU mask bit, and at these cancelling
@@ -38,10 +39,15 @@ def _round(a, precision):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-def _rounding_model(orc, spec, params, x, t, loss_name, precision, ml=None):
+def _rounding_model(orc, spec, params, x, t, loss_name, precision, ml=None, fp16_tables=False):
     """Network-weight gradients of the mean loss computed in float64 with the kernel's roundings."""
     q = lambda a: _round(a, precision)
-    x0 = q(orc.encode(x, params, max_level=ml).astype(np.float64))
+    enc_params = params
+    if fp16_tables:
+        n_net = spec["n_params_network"]
+        enc_params = params.copy()
+        enc_params[n_net:] = params[n_net:].astype(np.float16).astype(np.float32)
+    x0 = q(orc.encode(x, enc_params, max_level=ml).astype(np.float64))
     ws = [q(params[L["offset"]:L["offset"] + L["in"] * L["out"]].reshape(L["out"], L["in"]).astype(np.float64)) for L in spec["layers"]]
     hs = [x0]
     a = x0
@@ -75,7 +81,7 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-def _check(m, orc, spec, params, x, t, loss_name, precision, cuda, ml=None):
+def _check(m, orc, spec, params, x, t, loss_name, precision, cuda, ml=None, ema=False):
     import torch
 
     xd, td = torch.from_numpy(x).to(cuda), torch.from_numpy(t).to(cuda)
@@ -97,7 +103,7 @@ def _check(m, orc, spec, params, x, t, loss_name, precision, cuda, ml=None):
     untouched = ref_g[n_net:] == 0
     assert np.all(g[n_net:][untouched] == 0)
     # the same computation with the kernel's roundings, in float64
-    model = _rounding_model(orc, spec, params, x, t, loss_name, precision, ml)
+    model = _rounding_model(orc, spec, params, x, t, loss_name, precision, ml, fp16_tables=precision == "fp16" and not ema)
     for L, gm in zip(spec["layers"], model):
         gl = g[L["offset"]:L["offset"] + L["in"] * L["out"]].reshape(L["out"], L["in"])
         e = _rel(gl, gm)
@@ -142,7 +148,7 @@ def test_throughput_training_gradients(cuda, nlod_lib, precision):
     m.set_params(params)
     x = W.throughput_inputs(n, seed=15)
     t = np.random.default_rng(5).random((n, 3)).astype(np.float32)
-    _check(m, oracle.Oracle(enc, net, 10, 3), spec, params, x, t, "RelativeL2", precision, cuda)
+    _check(m, oracle.Oracle(enc, net, 10, 3), spec, params, x, t, "RelativeL2", precision, cuda, ema=True)
 
 
 def test_fused_training_reduces_loss_and_matches_fp32_trajectory(cuda, nlod_lib):
