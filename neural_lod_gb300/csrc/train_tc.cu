@@ -695,7 +695,9 @@ __global__ void __launch_bounds__(G * kGT + 32 + (ST ? kGT : 0), 1)
 // Encoding of the batch into X0 tiles in HBM, each tile laid out exactly as the fused kernel's
 // shared-memory A operand (128 rows x enc_width, K-major core matrices), so that one bulk copy
 // brings it in.  Full occupancy (128-thread CTAs) for the gather-bound grid levels.
-template <typename T, int NL>
+// TT: element type of the grid tables gathered (float: the FP32 parameters; __half: their FP16
+// copy, a.grid_h).  One table type per instantiation keeps the gather code at its register count.
+template <typename T, int NL, typename TT>
 __global__ void __launch_bounds__(kTile) k_encode_tiles(const __grid_constant__ ModelDesc d, const __grid_constant__ TrainTcArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     GridLevel* lvl_s = reinterpret_cast<GridLevel*>(smem);
@@ -718,13 +720,8 @@ __global__ void __launch_bounds__(kTile) k_encode_tiles(const __grid_constant__ 
         }
         __syncthreads();
         TcStore<T> st{reinterpret_cast<uint8_t*>(a.enc_tiles) + tile * x0_bytes, d.enc_width * 16u};
-        // FP16 form without an EMA: gather from the FP16 copy of the grid tables (the X0 operand is
-        // FP16 either way)
-        if (std::is_same<T, __half>::value && a.grid_h)
-            encode_tile_rows<NL>(d, lvl_s, static_cast<const __half*>(a.grid_h), in_s, in_ld, a.max_level_gpu, a.max_level, row0, kTile, tid,
-                                 kTile, st);
-        else
-            encode_tile_rows<NL>(d, lvl_s, a.params, in_s, in_ld, a.max_level_gpu, a.max_level, row0, kTile, tid, kTile, st);
+        const TT* table = std::is_same<TT, __half>::value ? static_cast<const TT*>(a.grid_h) : reinterpret_cast<const TT*>(a.params);
+        encode_tile_rows<NL>(d, lvl_s, table, in_s, in_ld, a.max_level_gpu, a.max_level, row0, kTile, tid, kTile, st);
     }
 }
 
@@ -821,8 +818,11 @@ cudaError_t launch_encode_tiles(const ModelDesc& d, const TrainTcArgs& a, int ki
     uint32_t blocks = (uint32_t)sm_count() * 16u;
     if (blocks > n_tiles) blocks = n_tiles;
     const size_t smem = kMaxGrids * kMaxLevels * sizeof(GridLevel) + (size_t)kTile * (d.n_input + 1) * 4u;
-    if (kind == 1) k_encode_tiles<__half, 2><<<blocks, kTile, smem, s>>>(d, a);
-    else if (kind == 2) k_encode_tiles<__nv_bfloat16, 2><<<blocks, kTile, smem, s>>>(d, a);
+    // the FP16 form gathers from the FP16 grid copy when the caller passes one (training values
+    // equal to the inference values: no EMA)
+    if (kind == 1 && a.grid_h) k_encode_tiles<__half, 2, __half><<<blocks, kTile, smem, s>>>(d, a);
+    else if (kind == 1) k_encode_tiles<__half, 2, float><<<blocks, kTile, smem, s>>>(d, a);
+    else if (kind == 2) k_encode_tiles<__nv_bfloat16, 2, float><<<blocks, kTile, smem, s>>>(d, a);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
