@@ -591,8 +591,6 @@ static int train_impl(nlod_module* m, void* stream, uint32_t n, const float* in,
         if (m->train_groups > 0) {
             // fused tensor-core step: one kernel for encoding, forward, loss and all gradients
             if (!m->loss_partial) m->loss_partial = dev_alloc<float>(kTrainPartials);
-            cuda_check(cudaMemsetAsync(m->loss_partial, 0, sizeof(float) * kTrainPartials, s), "memset");
-            cuda_check(cudaMemsetAsync(m->grads, 0, sizeof(float) * (size_t)m->n_params, s), "memset grads");
             TrainTcArgs t{};
             t.n = n;
             t.in = in;
@@ -608,6 +606,10 @@ static int train_impl(nlod_module* m, void* stream, uint32_t n, const float* in,
             t.loss_partial = m->loss_partial;
             // the FP16 grid copy holds the inference values: the training values only without an EMA
             t.grid_h = m->ema ? nullptr : m->grid_h;
+            // the encoding kernel zeroes the gradients (4-float tail, if any, by a memset)
+            t.zero_grads_n = (uint32_t)(m->n_params & ~size_t(3));
+            if (t.zero_grads_n != m->n_params)
+                cuda_check(cudaMemsetAsync(m->grads + t.zero_grads_n, 0, sizeof(float) * (m->n_params - t.zero_grads_n), s), "memset grads");
             const size_t enc_bytes = (size_t)n * m->d.enc_width * 2u;
             if (m->enc_tiles_bytes < enc_bytes) {
                 dev_free(m->enc_tiles);
@@ -619,7 +621,8 @@ static int train_impl(nlod_module* m, void* stream, uint32_t n, const float* in,
             t.enc_tiles = m->enc_tiles;
             cuda_check(launch_encode_tiles(m->d, t, m->op_kind(), s), "encoding");
             cuda_check(launch_train_tc(m->d, t, m->op_kind(), m->train_groups, m->status, s), "training step");
-            if (loss_out) cuda_check(launch_reduce_sum(m->loss_partial, kTrainPartials, loss_out, 1.0f, s), "loss");
+            // every CTA of the fused kernel wrote its partial: no memset, sum exactly those
+            if (loss_out) cuda_check(launch_reduce_sum(m->loss_partial, train_tc_blocks(n, m->train_groups), loss_out, 1.0f, s), "loss");
             m->grad_scale = loss_scale;
             if (run_opt) run_optimizer(m, s);
             return;

@@ -152,12 +152,15 @@ struct TrainTcArgs {
                                       // launch_encode_tiles and bulk-copied by the fused kernel
     const void* grid_h;               // nullable: FP16 copy of the (training = inference) grid tables,
                                       // read by launch_encode_tiles in the FP16 form
+    uint32_t zero_grads_n;            // launch_encode_tiles zeroes grads[0, zero_grads_n) (multiple of 4)
     uint32_t group_levels;            // grid levels a tile pipeline scatters itself when a
                                       // scatter team takes the rest (set by launch_train_tc)
 };
 // Tile pipelines per CTA that fit the network (0 = network not supported by the fused kernel).
 int train_tc_groups(const ModelDesc& d);
 cudaError_t launch_train_tc(const ModelDesc& d, const TrainTcArgs& a, int kind, int groups, uint32_t* status, cudaStream_t s);
+// CTAs launch_train_tc uses for a batch of n (each writes its loss_partial entry).
+uint32_t train_tc_blocks(uint32_t n, int groups);
 // Encodes the batch into a.enc_tiles (kind 1 = FP16, 2 = BF16).
 cudaError_t launch_encode_tiles(const ModelDesc& d, const TrainTcArgs& a, int kind, cudaStream_t s);
 

@@ -708,6 +708,10 @@ __global__ void __launch_bounds__(kTile) k_encode_tiles(const __grid_constant__ 
         const uint32_t g = i / kMaxLevels, l = i % kMaxLevels;
         if (l < d.grids[g].n_levels) lvl_s[i] = d.grids[g].levels[l];
     }
+    // the fused kernel accumulates into the gradient vector: zero it here, the stores overlapping
+    // the gathers' latency (no separate memset pass)
+    for (uint32_t i = blockIdx.x * kTile + tid; i < a.zero_grads_n / 4u; i += gridDim.x * kTile)
+        reinterpret_cast<float4*>(a.grads)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     const uint32_t n_tiles = a.n / kTile;
     const size_t x0_bytes = (size_t)kTile * d.enc_width * 2u;
     for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
@@ -766,15 +770,23 @@ uint32_t group_scatter_levels(const ModelDesc& d, int) {
     return nlev / 8u;
 }
 
+}  // namespace
+
+uint32_t train_tc_blocks(uint32_t n, int groups) {
+    const uint32_t n_tiles = n / kTile;
+    uint32_t blocks = (uint32_t)sm_count();
+    const uint32_t need = (n_tiles + groups - 1) / groups;
+    return blocks > need ? need : blocks;
+}
+
+namespace {
+
 template <typename T, int G, bool ST>
 cudaError_t launch_gs(const ModelDesc& d, const TrainTcArgs& a_in, uint32_t* status, cudaStream_t s) {
     TrainTcArgs a = a_in;
     a.group_levels = ST ? group_scatter_levels(d, G) : 0u;
     const TrainLayout L = train_layout(d, G);
-    const uint32_t n_tiles = a.n / kTile;
-    uint32_t blocks = (uint32_t)sm_count();
-    const uint32_t need = (n_tiles + G - 1) / G;
-    if (blocks > need) blocks = need;
+    const uint32_t blocks = train_tc_blocks(a.n, G);
     if (blocks == 0) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(k_train_tc<T, G, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
     if (e != cudaSuccess) return e;
