@@ -333,6 +333,9 @@ __global__ void __launch_bounds__(G * kGT + 32 + (ST ? kGT : 0), 1)
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    // Everything above reads only parameters; the X0 tiles, zeroed gradients and the batch come
+    // from the encoding kernel, which may still be finishing (programmatic dependent launch).
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
     // The CTA's tiles are one contiguous range (13 or 14 of 2048 tiles over 152 CTAs, where a
     // round-robin over all groups would give 16 to some CTAs and 12 to the rest); its groups take
@@ -708,6 +711,9 @@ __global__ void __launch_bounds__(kTile) k_encode_tiles(const __grid_constant__ 
         const uint32_t g = i / kMaxLevels, l = i % kMaxLevels;
         if (l < d.grids[g].n_levels) lvl_s[i] = d.grids[g].levels[l];
     }
+    // the fused training kernel may start its set-up now (programmatic dependent launch); it waits
+    // for this grid's completion before touching what it writes
+    asm volatile("griddepcontrol.launch_dependents;");
     // the fused kernel accumulates into the gradient vector: zero it here, the stores overlapping
     // the gathers' latency (no separate memset pass)
     for (uint32_t i = blockIdx.x * kTile + tid; i < a.zero_grads_n / 4u; i += gridDim.x * kTile)
@@ -790,8 +796,18 @@ cudaError_t launch_gs(const ModelDesc& d, const TrainTcArgs& a_in, uint32_t* sta
     if (blocks == 0) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(k_train_tc<T, G, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
     if (e != cudaSuccess) return e;
-    k_train_tc<T, G, ST><<<blocks, G * kGT + 32 + (ST ? kGT : 0), L.total, s>>>(d, a, status);
-    return cudaGetLastError();
+    // programmatic dependent launch: the set-up overlaps the encoding kernel's last wave
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(G * kGT + 32 + (ST ? kGT : 0));
+    cfg.dynamicSmemBytes = L.total;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_train_tc<T, G, ST>, d, a, status);
 }
 
 template <typename T, int G>
