@@ -93,6 +93,9 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
     const uint32_t gtid = tid & (kGroupThreads - 1);
     const uint32_t quarter = warp & 3u;          // TMEM lane quarter this warp may access
     const uint32_t bar_id = 1u + grp;
+    // A CTA without a tile (device row counts below the launch size: the renderer's late rounds)
+    // leaves before staging weights and allocating TMEM.  The test is uniform over the CTA.
+    if (blockIdx.x * G >= forward_rows(a) / kTcTile) return;
 
     // ---- set-up: barriers, TMEM, resident weights ----
     if (tid == 0) {
