@@ -9,7 +9,9 @@
 //       forward l < L-1 : ReLU, hidden activations H[l+1] kept in shared memory;
 //       forward L-1     : output activation, loss value, dL/dy (per element, unscaled) -> DZ;
 //       backward b >= 1 : dL/dH[b] * act'(H[b]) = delta of layer b-1, written over H[b];
-//       backward 0      : dL/dX0 -> grid-table gradients (warp-aggregated FP32 atomics).
+//       backward 0      : dL/dX0 -> grid-table gradients (FP32 reductions, one per corner or one
+//                         16-byte reduction per aligned x-adjacent entry pair; most levels are
+//                         handed to a scatter team, see ST below).
 //   * the MMA warp's elected thread serves the groups' READY signals in turn: per job it issues
 //     tcgen05.mma (M = 128 rows of the tile, FP32 accumulate in the group's TMEM columns) and, for
 //     a backward job, the weight-gradient MMA dW_b += delta_b^T A_b (M = 64, contraction over the
@@ -46,7 +48,10 @@ constexpr int kTile = 128;
 constexpr int kGT = 128;                         // threads of a group
 constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 constexpr uint32_t kHBytes = kTile * 64u * 2u;   // one hidden activation buffer (128 x 64, 16-bit)
-constexpr bool kScatterAggregate = false;        // one atomic per corner (see grid_level_scatter8)
+// Merging the lanes of a warp that hit the same entry before the reduction (grid_level_scatter8's
+// AGG form) costs eight warp matches per level and pays only for spatially coherent batches; the
+// training batches here are random, so every corner goes straight to the L2.
+constexpr bool kScatterAggregate = false;
 
 __host__ __device__ inline uint32_t al(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
 
