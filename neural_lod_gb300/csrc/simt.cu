@@ -14,6 +14,7 @@
 
 #include <cstdint>
 
+#include "activation.cuh"
 #include "desc.h"
 #include "encoding.cuh"
 #include "kernels.h"
@@ -24,25 +25,6 @@ namespace {
 
 constexpr int kTile = 64;
 constexpr int kThreads = 256;
-
-__device__ __forceinline__ float apply_act(int32_t act, float v) {
-    switch (act) {
-        case ACT_RELU: return v > 0.f ? v : 0.f;
-        case ACT_SIGMOID: return 1.0f / (1.0f + expf(-v));
-        case ACT_EXP: return expf(v);
-        default: return v;
-    }
-}
-
-// Derivative of the output activation from its output value y (common_device.h:341-352).
-__device__ __forceinline__ float act_grad_from_output(int32_t act, float y) {
-    switch (act) {
-        case ACT_RELU: return y > 0.f ? 1.f : 0.f;
-        case ACT_SIGMOID: return y * (1.f - y);
-        case ACT_EXP: return y;
-        default: return 1.f;
-    }
-}
 
 // Per-element loss value (already divided by n_total) and d loss / d prediction (scaled).
 __device__ __forceinline__ float loss_eval(int32_t kind, float pred, float target, float inv_n_total, float loss_scale, float& grad) {
@@ -214,13 +196,14 @@ __global__ void __launch_bounds__(kThreads) k_forward_simt(const __grid_constant
             LayerBlock<W> lb;
             lb.compute(cur, ld_cur, K, w_s, W, 0);
             __syncthreads();  // everyone done reading cur / w_s
+            const ReluOrNone act{d.act == ACT_RELU};
 #pragma unroll
             for (int r = 0; r < LayerBlock<W>::RPT; ++r) {
                 float4 v;
-                v.x = apply_act(d.act, lb.acc[r][0]);
-                v.y = apply_act(d.act, lb.acc[r][1]);
-                v.z = apply_act(d.act, lb.acc[r][2]);
-                v.w = apply_act(d.act, lb.acc[r][3]);
+                v.x = act(lb.acc[r][0]);
+                v.y = act(lb.acc[r][1]);
+                v.z = act(lb.acc[r][2]);
+                v.w = act(lb.acc[r][3]);
                 *reinterpret_cast<float4*>(nxt + lb.row(r) * ld_nxt + 4 * lb.cg()) = v;
                 if (a.hidden) {
                     *reinterpret_cast<float4*>(a.hidden + ((size_t)l * a.n + row0 + lb.row(r)) * W + 4 * lb.cg()) = v;
@@ -241,7 +224,7 @@ __global__ void __launch_bounds__(kThreads) k_forward_simt(const __grid_constant
             const uint32_t grow = row0 + r;
             float yv[4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) yv[j] = apply_act(d.out_act, lb.acc[0][j]);
+            for (int j = 0; j < 4; ++j) yv[j] = act_fwd(d.out_act, lb.acc[0][j]);
             if (a.y) *reinterpret_cast<float4*>(a.y + (size_t)grow * 16 + 4 * lb.cg()) = make_float4(yv[0], yv[1], yv[2], yv[3]);
 #pragma unroll
             for (int j = 0; j < 4; ++j) {

@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
             if (!last) {
                 // hidden epilogue: each warp converts all W columns of its 32 rows
                 const uint32_t out_sbo = (uint32_t)W * 16u;
+                const ReluOrNone act{d.act == ACT_RELU};
 #pragma unroll
                 for (uint32_t col = 0; col < (uint32_t)W; col += 32) {
                     uint32_t r[32];
@@ -201,10 +202,10 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
 #pragma unroll
                     for (uint32_t j = 0; j < 4; ++j) {
                         uint4 pk;
-                        pk.x = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * j + 0])), act_fwd(d.act, __uint_as_float(r[8 * j + 1])));
-                        pk.y = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * j + 2])), act_fwd(d.act, __uint_as_float(r[8 * j + 3])));
-                        pk.z = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * j + 4])), act_fwd(d.act, __uint_as_float(r[8 * j + 5])));
-                        pk.w = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * j + 6])), act_fwd(d.act, __uint_as_float(r[8 * j + 7])));
+                        pk.x = Op::pack2(act(__uint_as_float(r[8 * j + 0])), act(__uint_as_float(r[8 * j + 1])));
+                        pk.y = Op::pack2(act(__uint_as_float(r[8 * j + 2])), act(__uint_as_float(r[8 * j + 3])));
+                        pk.z = Op::pack2(act(__uint_as_float(r[8 * j + 4])), act(__uint_as_float(r[8 * j + 5])));
+                        pk.w = Op::pack2(act(__uint_as_float(r[8 * j + 6])), act(__uint_as_float(r[8 * j + 7])));
                         *reinterpret_cast<uint4*>(a_tile + tc::kmajor_offset(row, col + 8u * j, out_sbo)) = pk;
                     }
                 }
@@ -216,8 +217,9 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
                 const size_t grow = (size_t)row0 + row;
                 if (a.out) {
                     // written once: streaming stores (evict-first in L2)
-                    for (uint32_t c = 0; c < d.n_output; ++c)
-                        __stcs(a.out + grow * d.n_output + c, act_fwd(d.out_act, __uint_as_float(r[c])));
+#pragma unroll
+                    for (uint32_t c = 0; c < 16u; ++c)
+                        if (c < d.n_output) __stcs(a.out + grow * d.n_output + c, act_fwd(d.out_act, __uint_as_float(r[c])));
                 }
                 if (a.y) {
                     float4* yv = reinterpret_cast<float4*>(a.y + grow * 16);

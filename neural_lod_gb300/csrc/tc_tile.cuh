@@ -1,5 +1,5 @@
 // Helpers shared by the tensor-core kernels (query and training): per-group named barriers,
-// the store of encoded features into a K-major operand tile, and the activations.
+// and the store of encoded features into a K-major operand tile.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -7,6 +7,7 @@
 
 #include <cstdint>
 
+#include "activation.cuh"
 #include "desc.h"
 #include "tc_common.cuh"
 
@@ -64,15 +65,6 @@ struct TcStore {
         *reinterpret_cast<uint16_t*>(tile + tc::kmajor_offset(r, col, sbo)) = tc::OpType<T>::pack1(v);
     }
 };
-
-__device__ __forceinline__ float act_fwd(int32_t act, float v) {
-    switch (act) {
-        case ACT_RELU: return v > 0.f ? v : 0.f;
-        case ACT_SIGMOID: return 1.0f / (1.0f + expf(-v));
-        case ACT_EXP: return expf(v);
-        default: return v;
-    }
-}
 
 
 }  // namespace nlod

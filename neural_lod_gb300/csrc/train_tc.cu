@@ -130,15 +130,6 @@ __device__ __forceinline__ float loss_unit(int32_t kind, float pred, float targe
     }
 }
 
-__device__ __forceinline__ float out_act_grad(int32_t act, float y) {
-    switch (act) {
-        case ACT_RELU: return y > 0.f ? 1.f : 0.f;
-        case ACT_SIGMOID: return y * (1.f - y);
-        case ACT_EXP: return y;
-        default: return 1.f;
-    }
-}
-
 // Saturating conversion for the 16-bit delta buffers.
 __device__ __forceinline__ float sat16(float v) { return fminf(fmaxf(v, -65504.f), 65504.f); }
 
@@ -463,6 +454,7 @@ __global__ void __launch_bounds__(G * kGT + 32 + (ST ? kGT : 0), 1)
                     }
                     // hidden layer j: activation -> H[j+1]
                     uint8_t* h = hbuf(j + 1);
+                    const ReluOrNone act{d.act == ACT_RELU};
 #pragma unroll
                     for (uint32_t col = 0; col < 64u; col += 32) {
                         uint32_t r[32];
@@ -471,10 +463,10 @@ __global__ void __launch_bounds__(G * kGT + 32 + (ST ? kGT : 0), 1)
 #pragma unroll
                         for (uint32_t q = 0; q < 4; ++q) {
                             uint4 pk;
-                            pk.x = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * q + 0])), act_fwd(d.act, __uint_as_float(r[8 * q + 1])));
-                            pk.y = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * q + 2])), act_fwd(d.act, __uint_as_float(r[8 * q + 3])));
-                            pk.z = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * q + 4])), act_fwd(d.act, __uint_as_float(r[8 * q + 5])));
-                            pk.w = Op::pack2(act_fwd(d.act, __uint_as_float(r[8 * q + 6])), act_fwd(d.act, __uint_as_float(r[8 * q + 7])));
+                            pk.x = Op::pack2(act(__uint_as_float(r[8 * q + 0])), act(__uint_as_float(r[8 * q + 1])));
+                            pk.y = Op::pack2(act(__uint_as_float(r[8 * q + 2])), act(__uint_as_float(r[8 * q + 3])));
+                            pk.z = Op::pack2(act(__uint_as_float(r[8 * q + 4])), act(__uint_as_float(r[8 * q + 5])));
+                            pk.w = Op::pack2(act(__uint_as_float(r[8 * q + 6])), act(__uint_as_float(r[8 * q + 7])));
                             *reinterpret_cast<uint4*>(h + tc::kmajor_offset(row, col + 8u * q, 1024u)) = pk;
                         }
                     }
@@ -490,7 +482,7 @@ __global__ void __launch_bounds__(G * kGT + 32 + (ST ? kGT : 0), 1)
                         if (c < d.n_output) {
                             const float y = act_fwd(d.out_act, __uint_as_float(r[c]));
                             loss_acc += loss_unit(a.loss_kind, y, __ldg(a.target + grow * d.n_output + c), gv) * a.inv_n_total;
-                            gv *= out_act_grad(d.out_act, y);
+                            gv *= act_grad_from_output(d.out_act, y);
                         }
                         dzv[c] = sat16(gv);
                     }
