@@ -2,11 +2,9 @@
 // value (tiny-cuda-nn include/tiny-cuda-nn/common_device.h:68-230 and :341-352), shared by the
 // plain FP32 kernels and the tensor-core kernels.
 //
-// Element loops take the activation through with_act(), which branches once on the activation
-// code and runs the loop body with the activation fixed at compile time.  A switch on the code
-// inside the loop measured about ten times slower than the fixed form: one 128-row tile's
-// 64-column hidden epilogue in the tensor-core query took 3.8 us with the per-element switch
-// against 0.4 us with the activation fixed.
+// Hidden-layer loops take the activation through ReluOrNone, a flag tested per element, not through
+// a switch on the activation code: in the tensor-core query one 128-row tile's 64-column hidden
+// epilogue took 3.8 us with the per-element switch against 0.4 us with the flag.
 #pragma once
 
 #include <cstdint>
@@ -34,28 +32,9 @@ __device__ __forceinline__ float act_grad_from_output(int32_t act, float y) {
     }
 }
 
-// One activation as a compile-time constant (act_fwd folds to its case).
-template <int32_t A>
-struct FixedAct {
-    static constexpr int32_t kind = A;
-    __device__ __forceinline__ float operator()(float v) const { return act_fwd(A, v); }
-    __device__ __forceinline__ float grad_from_output(float y) const { return act_grad_from_output(A, y); }
-};
-
-// body(FixedAct<act>{}) for the runtime activation code act (uniform over the caller's threads).
-template <typename Body>
-__device__ __forceinline__ void with_act(int32_t act, Body&& body) {
-    switch (act) {
-        case ACT_RELU: body(FixedAct<ACT_RELU>{}); break;
-        case ACT_SIGMOID: body(FixedAct<ACT_SIGMOID>{}); break;
-        case ACT_EXP: body(FixedAct<ACT_EXP>{}); break;
-        default: body(FixedAct<ACT_NONE>{}); break;
-    }
-}
-
 // The hidden activation (ReLU or identity, the two that model descriptions accept) chosen by a
-// flag: exactly act_fwd's two cases, NaN included, in one compiled copy of the loop (a copy per
-// activation spilled registers in the tensor-core kernels).
+// flag: exactly act_fwd's two cases, NaN included, in one compiled copy of the loop (a loop copy
+// per activation made the tensor-core kernels spill registers).
 struct ReluOrNone {
     bool relu;
     __device__ __forceinline__ float operator()(float v) const { return (relu && !(v > 0.f)) ? 0.f : v; }
