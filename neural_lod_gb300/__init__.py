@@ -44,6 +44,11 @@ def _stream_ptr(stream) -> int | None:
     import torch
 
     if stream is None:
+        # torch's current stream on the current device, read as a raw handle where torch offers
+        # that (it skips building a Stream object on every call of a small query)
+        raw = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+        if raw is not None:
+            return raw(torch.cuda.current_device()) or None
         return torch.cuda.current_stream().cuda_stream or None
     if isinstance(stream, int):
         return stream or None

@@ -6,10 +6,30 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "desc.h"
 
 namespace nlod {
+
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` on the current device.  The
+// attribute is set only when the limit recorded for (kernel, device) is lower, so that repeated
+// launches of small batches do not pay for a cudaFuncSetAttribute call each.
+inline cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> limits;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& cur = limits[{kernel, dev}];
+    if (cur >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
 
 // Inputs shared by every forward-style launch.
 struct ForwardArgs {

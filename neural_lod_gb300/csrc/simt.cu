@@ -428,7 +428,7 @@ int num_sms() {
 
 template <typename K>
 cudaError_t set_smem(K kernel, size_t bytes) {
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return ensure_dynamic_smem((const void*)kernel, bytes);
 }
 
 }  // namespace

@@ -293,7 +293,7 @@ cudaError_t launch_variant(const ModelDesc& d, const ForwardArgs& a, uint32_t* s
     const uint32_t need = (n_tiles + G - 1) / G;
     if (blocks > need) blocks = need;
     if (blocks == 0) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_forward_tc<W, T, G, NL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_forward_tc<W, T, G, NL>, bytes);
     if (e != cudaSuccess) return e;
     k_forward_tc<W, T, G, NL><<<blocks, G * kGroupThreads, bytes, s>>>(d, a, status);
     return cudaGetLastError();

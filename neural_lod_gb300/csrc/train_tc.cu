@@ -791,7 +791,7 @@ cudaError_t launch_gs(const ModelDesc& d, const TrainTcArgs& a_in, uint32_t* sta
     const TrainLayout L = train_layout(d, G);
     const uint32_t blocks = train_tc_blocks(a.n, G);
     if (blocks == 0) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_train_tc<T, G, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_train_tc<T, G, ST>, L.total);
     if (e != cudaSuccess) return e;
     // programmatic dependent launch: the set-up overlaps the encoding kernel's last wave
     cudaLaunchConfig_t cfg{};
