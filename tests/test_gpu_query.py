@@ -83,6 +83,20 @@ def test_visibility16_query(cuda, nlod_lib, precision):
     _check(out, ref, precision)
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16"])
+def test_identity_hidden_activation(cuda, nlod_lib, precision):
+    """Hidden activation "None": the identity branch of every hidden epilogue."""
+    import torch
+
+    enc, net = W.throughput_configs()
+    net = dict(net, activation="None", output_activation="Sigmoid")
+    m, orc, params = _net((enc, net), 10, 3, precision)
+    x = W.throughput_inputs(4096, seed=21)
+    ref = orc.forward(x, params)
+    out = m.inference(torch.from_numpy(x).to(cuda)).cpu().numpy()
+    _check(out, ref, precision)
+
+
 @pytest.mark.parametrize("precision", ["fp32", "fp16"])
 def test_width128_sh8_config(cuda, nlod_lib, precision):
     """The shipped arcade throughput configuration shape: 7-level grid (base 8, scale 2),

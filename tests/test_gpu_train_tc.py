@@ -49,10 +49,12 @@ def _rounding_model(orc, spec, params, x, t, loss_name, precision, ml=None, fp16
         enc_params[n_net:] = params[n_net:].astype(np.float16).astype(np.float32)
     x0 = q(orc.encode(x, enc_params, max_level=ml).astype(np.float64))
     ws = [q(params[L["offset"]:L["offset"] + L["in"] * L["out"]].reshape(L["out"], L["in"]).astype(np.float64)) for L in spec["layers"]]
+    relu = spec["act"] == 1
     hs = [x0]
     a = x0
     for w in ws[:-1]:
-        a = q(np.maximum((a.astype(np.float32) @ w.T.astype(np.float32)).astype(np.float64), 0.0))
+        a = (a.astype(np.float32) @ w.T.astype(np.float32)).astype(np.float64)
+        a = q(np.maximum(a, 0.0) if relu else a)
         hs.append(a)
     z = a @ ws[-1].T
     no = spec["n_output"]
@@ -73,7 +75,7 @@ def _rounding_model(orc, spec, params, x, t, loss_name, precision, ml=None, fp16
     for l in range(len(ws) - 1, -1, -1):
         grads[l] = d.T @ hs[l]
         if l > 0:
-            d = q((d @ ws[l]) * (hs[l] > 0))
+            d = q((d @ ws[l]) * (hs[l] > 0)) if relu else q(d @ ws[l])
     return [gr / (x.shape[0] * no) for gr in grads]
 
 
@@ -173,3 +175,20 @@ def test_fused_training_reduces_loss_and_matches_fp32_trajectory(cuda, nlod_lib)
         m.sync_status()
     assert losses["fp16"][1] < 0.8 * losses["fp16"][0]
     assert abs(losses["fp16"][1] - losses["fp32"][1]) <= 0.05 * losses["fp32"][1]
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+def test_identity_hidden_activation(cuda, nlod_lib, precision):
+    """Hidden activation "None" (the hidden epilogues' identity branch) on the visibility network
+    shape, with a small weight scale so that the unbounded pre-activations stay in FP16 range."""
+    n = 4096
+    enc, net = W.visibility_configs(16)
+    net = dict(net, activation="None")
+    spec = oracle.model_spec(enc, net, 6, 1)
+    assert spec["act"] == 0
+    params = W.test_params(spec, seed=6, grid_scale=0.3)
+    m = NetworkWithInputEncoding(6, 1, enc, net, loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER, precision=precision)
+    m.set_params(params)
+    x, _, _ = W.visibility_inputs(n, seed=16)
+    t = (np.random.default_rng(6).random((n, 1)) < 0.4).astype(np.float32)
+    _check(m, oracle.Oracle(enc, net, 6, 1), spec, params, x, t, "BinaryCrossEntropy", precision, cuda)
