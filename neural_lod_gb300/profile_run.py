@@ -21,7 +21,7 @@ sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["query", "train", "visq", "render", "voxelize", "sampler"])
+    ap.add_argument("what", choices=["query", "train", "train_thr", "visq", "render", "voxelize", "sampler"])
     ap.add_argument("--precision", default="fp16")
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--iters", type=int, default=3)
@@ -109,6 +109,18 @@ def main():
         torch.cuda.synchronize()
         print("ok voxelize", n)
         return
+    elif a.what == "train_thr":
+        # the throughput network's training step: 2^20 samples, RelativeL2, Ema(0.95) of
+        # ExponentialDecay(Adam) (the bench's throughput_train workload)
+        n = a.n or (1 << 20)
+        enc, net = W.throughput_configs()
+        m = N.NetworkWithInputEncoding(10, 3, enc, net, loss=W.THROUGHPUT_LOSS, optimizer=W.THROUGHPUT_OPTIMIZER,
+                                       precision=a.precision)
+        m.set_params(W.xavier_params(N.layout(enc, net, 10, 3), seed=10))
+        x = torch.from_numpy(W.throughput_inputs(n, seed=4)).to(dev)
+        td = torch.from_numpy(np.random.default_rng(4).random((n, 3)).astype(np.float32)).to(dev)
+        for _ in range(a.iters):
+            m.training_step(x, td)
     else:
         n = a.n or W.WORKLOADS["visibility_train"]["batch"]
         enc, net = W.visibility_configs(16)
