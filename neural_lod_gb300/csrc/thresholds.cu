@@ -103,7 +103,9 @@ __global__ void __launch_bounds__(128) k_optimal_thresholds(const float* __restr
         for (uint32_t t = 0; t < kThresholds; ++t)
             if (sc[t] > best) { best = sc[t]; opt = t; }
         uint32_t eq = 0;
-        while (opt + eq < kThresholds && fabsf(sc[opt + eq] - sc[opt]) < 1e-4f) ++eq;
+        // the reference compares the float difference with the double 1e-4 (neural_lod_learning.cu:
+        // 257); 1e-4f is the largest float below 1e-4, so "<= 1e-4f" is the same test in float
+        while (opt + eq < kThresholds && fabsf(sc[opt + eq] - sc[opt]) <= 1e-4f) ++eq;
         opt += eq / 2;
         out[v] = opt / (float)(kThresholds - 1);
     }

@@ -970,7 +970,9 @@ void orc_optimal_thresholds(const float* truth, const float* proba, uint32_t n_s
         for (int k = 0; k < T; ++k)
             if (sc[k] > best) { best = sc[k]; opt = k; }
         int eq = 0;
-        while (opt + eq < T && fabsf(sc[opt + eq] - sc[opt]) < 1e-4f) ++eq;
+        /* neural_lod_learning.cu:257 compares with the double 1e-4; 1e-4f is the largest float
+           below it, so "<= 1e-4f" is the same test */
+        while (opt + eq < T && fabsf(sc[opt + eq] - sc[opt]) <= 1e-4f) ++eq;
         opt += eq / 2;
         out[v] = opt / (float)(T - 1);
     }
