@@ -93,6 +93,9 @@ def test_sh_padding_goes_first_and_composite_pads_last_nested():
     ({"otype": "HashGrid"}, {"otype": "FullyFusedMLP", "n_neurons": 64}, 3, 17, "n_output_dims"),
     ({"otype": "Composite", "nested": [{"otype": "HashGrid", "n_dims_to_encode": 4}]}, {"otype": "FullyFusedMLP"}, 3, 1, "more dims"),
     ("{not json", {"otype": "FullyFusedMLP"}, 3, 1, "json"),
+    # the fused kernels' hidden epilogues implement exactly these two activations
+    ({"otype": "HashGrid"}, {"otype": "FullyFusedMLP", "n_neurons": 64, "activation": "Sigmoid"}, 3, 1, "ReLU or None"),
+    ({"otype": "HashGrid"}, {"otype": "FullyFusedMLP", "n_neurons": 64, "activation": "Exponential"}, 3, 1, "ReLU or None"),
 ])
 def test_bad_configs_are_rejected(nlod_lib, enc, net, n_in, n_out, msg):
     with pytest.raises(NlodError) as e:
@@ -113,3 +116,27 @@ def test_module_create_rejects_bad_config_before_touching_the_gpu(nlod_lib):
     with pytest.raises(NlodError):
         NetworkWithInputEncoding(3, 1, {"otype": "HashGrid"}, {"otype": "FullyFusedMLP", "n_neurons": 64},
                                  optimizer={"otype": "Shampoo"})
+
+
+def test_entry_points_reject_null_arguments_before_touching_the_gpu(nlod_lib):
+    """Every call returns NLOD_ERR_INVALID (1) with a message for a NULL module or buffer, and
+    never throws across the boundary."""
+    import ctypes as C
+
+    L = nlod_lib
+    out = C.c_void_p()
+    calls = {
+        "nlod_inference": lambda: L.nlod_inference(None, None, 128, None, None),
+        "nlod_inference_host": lambda: L.nlod_inference_host(None, None, 128, None, None),
+        "nlod_training_step": lambda: L.nlod_training_step(None, None, 128, None, None, None),
+        "nlod_forward": lambda: L.nlod_forward(None, None, 128, None, None, None),
+        "nlod_optimizer_step": lambda: L.nlod_optimizer_step(None, None),
+        "nlod_autotune": lambda: L.nlod_autotune(None, None, 128, None, None),
+        "nlod_serialize": lambda: L.nlod_serialize(None, 1, C.byref(out)),
+        "nlod_deserialize": lambda: L.nlod_deserialize(None, b"{}"),
+        "nlod_set_params": lambda: L.nlod_set_params(None, None, 0, 0),
+    }
+    for name, call in calls.items():
+        assert call() == 1, name
+        assert L.nlod_last_error(), name
+    assert L.nlod_n_params(None) == 0
