@@ -135,6 +135,15 @@ def test_entry_points_reject_null_arguments_before_touching_the_gpu(nlod_lib):
         "nlod_serialize": lambda: L.nlod_serialize(None, 1, C.byref(out)),
         "nlod_deserialize": lambda: L.nlod_deserialize(None, b"{}"),
         "nlod_set_params": lambda: L.nlod_set_params(None, None, 0, 0),
+        "nlod_lod_grid_create": lambda: L.nlod_lod_grid_create(None, 64, 4, None, C.byref(out)),
+        "nlod_first_active_voxel": lambda: L.nlod_first_active_voxel(None, 0, None, 128, *([None] * 8)),
+        "nlod_voxelize": lambda: L.nlod_voxelize(None, 10, 64, None, None, None, None),
+        "nlod_renderer_create": lambda: L.nlod_renderer_create(None, None, None, None, C.byref(out)),
+        "nlod_render_frame": lambda: L.nlod_render_frame(None, None, None, None),
+        "nlod_optimal_thresholds": lambda: L.nlod_optimal_thresholds(None, None, 16, 4, 0, C.c_float(1.0), None, None),
+        "nlod_morton_voxels": lambda: L.nlod_morton_voxels(None, 64, None, 0, None, None),
+        "nlod_sample_visibility": lambda: L.nlod_sample_visibility(None, None, None, 0, 128, None, None, None, None),
+        "nlod_trace_visibility": lambda: L.nlod_trace_visibility(None, None, None, 128, None, None),
     }
     for name, call in calls.items():
         assert call() == 1, name
