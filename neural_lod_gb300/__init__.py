@@ -107,6 +107,7 @@ class NetworkWithInputEncoding:
 
     # ---- grid level masking (GridEncoding::set_max_level / set_max_level_gpu) ---------------
     def set_max_level(self, value: float) -> None:
+        """One level fraction in [0,1] for every element (levels above it encode as zero)."""
         check(self._lib.nlod_set_max_level(self._m, float(value)))
 
     def set_max_level_gpu(self, per_element) -> None:
@@ -116,6 +117,9 @@ class NetworkWithInputEncoding:
 
     # ---- compute ----------------------------------------------------------------------------
     def inference(self, x, out=None, stream=None):
+        """network->inference(stream, X, Y): x cuda float32 [n][n_input_dims], n a multiple of 128;
+        returns out, cuda float32 [n][n_output_dims] (asynchronous on `stream`, torch's current
+        stream by default)."""
         import torch
 
         n = x.shape[0]
@@ -149,6 +153,8 @@ class NetworkWithInputEncoding:
         return loss_out
 
     def optimizer_step(self, stream=None) -> None:
+        """Applies the optimizer to the gradients of the last forward/backward (Trainer's
+        optimizer step: loss scale divided out, Adam, ExponentialDecay and EMA wrappers)."""
         check(self._lib.nlod_optimizer_step(self._m, _stream_ptr(stream)))
 
     def forward(self, x, out=None, stream=None):
@@ -163,6 +169,8 @@ class NetworkWithInputEncoding:
         return out, _Ctx(self._lib, ctx)
 
     def backward(self, ctx, x, dL_dout, stream=None) -> None:
+        """Accumulates parameter gradients from dL/d(output) [n][n_output_dims] into the module's
+        gradient vector (read with get_params("gradients"))."""
         check(self._lib.nlod_backward(self._m, _stream_ptr(stream), ctx.handle, _ptr(x), _ptr(dL_dout)))
 
     # ---- kernel variants / autotuning ------------------------------------------------------
@@ -188,6 +196,8 @@ class NetworkWithInputEncoding:
         return self.kernel_variant
 
     def sync_status(self, stream=None) -> None:
+        """Synchronises `stream` and raises NlodError if a kernel reported a device-side error
+        (for example a wait that gave up) since the last check."""
         check(self._lib.nlod_sync_status(self._m, _stream_ptr(stream)))
 
     # ---- parameters -------------------------------------------------------------------------
@@ -201,6 +211,9 @@ class NetworkWithInputEncoding:
         return buf
 
     def set_params(self, params) -> None:
+        """Trainer::set_params_full_precision: the FP32 vector (network then encoding) from a numpy
+        array or a cuda tensor; the EMA (inference) weights and the FP16/BF16 copies are set to it
+        too."""
         import numpy as np
 
         if hasattr(params, "is_cuda") and params.is_cuda:
@@ -223,6 +236,9 @@ class NetworkWithInputEncoding:
 
     # ---- checkpoints (Trainer::serialize / deserialize JSON) --------------------------------
     def serialize(self, half_precision: bool = True) -> str:
+        """Trainer::serialize's parameter fields as JSON text: n_params, params_type and the
+        inference parameters (the EMA when there is one) as `params_binary` bytes, FP16 when
+        half_precision (as tiny-cuda-nn's half build writes them), else FP32."""
         p = C.c_void_p()
         check(self._lib.nlod_serialize(self._m, 1 if half_precision else 0, C.byref(p)))
         try:
@@ -231,6 +247,7 @@ class NetworkWithInputEncoding:
             self._lib.nlod_free_string(p)
 
     def deserialize(self, data: str | dict) -> None:
+        """Trainer::deserialize: loads what serialize() (or tiny-cuda-nn's trainer) wrote."""
         s = data if isinstance(data, str) else _json.dumps(data)
         check(self._lib.nlod_deserialize(self._m, s.encode()))
 
