@@ -149,3 +149,27 @@ def test_entry_points_reject_null_arguments_before_touching_the_gpu(nlod_lib):
         assert call() == 1, name
         assert L.nlod_last_error(), name
     assert L.nlod_n_params(None) == 0
+
+
+def test_last_error_is_per_thread(nlod_lib):
+    """nlod_last_error() reports the calling thread's last failure only."""
+    import threading
+
+    L = nlod_lib
+    seen = {}
+
+    def worker():
+        assert L.nlod_inference(None, None, 128, None, None) == 1
+        seen["worker"] = L.nlod_last_error()
+
+    t = threading.Thread(target=worker)
+    t.start()
+    t.join()
+    assert seen["worker"] == b"module is NULL"
+    # this thread made no failing call since its own last one: a different message or none
+    assert L.nlod_set_params(None, None, 0, 0) == 1
+    mine = L.nlod_last_error()
+    t2 = threading.Thread(target=worker)
+    t2.start()
+    t2.join()
+    assert L.nlod_last_error() == mine
