@@ -173,9 +173,13 @@ NLOD_API int nlod_training_step(nlod_module* m, void* stream, uint32_t n, const 
  * it until the process exits, instead of a cudaMalloc'ed workspace, and the call itself allocates
  * nothing.  A batch whose intermediates do not fit is rejected with NLOD_ERR_INVALID and a message
  * giving the largest batch this network can use (about 10k elements for a 48-wide encoding with two
- * 64-wide hidden layers).  The first call on a device looks up the scratch's device address for that
- * device; make that first call before any stream capture.  All calls share the one scratch, so calls
- * that overlap on the GPU (other streams or threads) race on it.
+ * 64-wide hidden layers).  The first call in a device's context is the set-up: it looks up the
+ * scratch's device address and, under CUDA's lazy module loading (the default), that first lookup
+ * and the first launches load the scratch and the step's kernels, which takes device memory once.
+ * Make that first call at start-up, outside the no-allocation region and before any stream capture;
+ * from the second call on nothing is allocated.  The same holds again after cudaDeviceReset, which
+ * gives the device a new context.  All calls share the one scratch and it keeps the last call's
+ * contents, so calls that overlap on the GPU (other streams or threads) race on it.
  */
 NLOD_API int nlod_training_step_noalloc(nlod_module* m, void* stream, uint32_t n, const float* in,
                                         const float* target, float* loss_out);

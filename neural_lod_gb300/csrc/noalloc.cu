@@ -12,7 +12,6 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
-#include <mutex>
 
 #include "kernels.h"
 
@@ -22,28 +21,19 @@ namespace {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
-
 }  // namespace
 
-// Device address of the scratch on the current device.  The host-side name of the array is only a
-// stand-in, so the address is looked up with cudaGetSymbolAddress once per device (with that
-// device current) and cached.
+// Device address of the scratch in the current device's context.  The host-side name of the array
+// is only a stand-in, so the address is looked up with cudaGetSymbolAddress, with that device
+// current, on every call: once the array is loaded the lookup is a table read, and a context
+// created again after cudaDeviceReset gets its own array and address rather than a stale one.
+// Under CUDA's lazy module loading the first lookup in a context loads this file's module, which
+// is when the array takes its device memory.
 cudaError_t noalloc_scratch(void** ptr, size_t* bytes) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_addr[dev] = p;
-    }
-    *ptr = g_addr[dev];
+    *ptr = p;
     *bytes = kNoAllocScratchBytes;
     return cudaSuccess;
 }

@@ -129,6 +129,8 @@ def test_entry_points_reject_null_arguments_before_touching_the_gpu(nlod_lib):
         "nlod_inference": lambda: L.nlod_inference(None, None, 128, None, None),
         "nlod_inference_host": lambda: L.nlod_inference_host(None, None, 128, None, None),
         "nlod_training_step": lambda: L.nlod_training_step(None, None, 128, None, None, None),
+        "nlod_training_step_noalloc": lambda: L.nlod_training_step_noalloc(None, None, 128, None, None, None),
+        "nlod_training_step_noalloc (batch 100)": lambda: L.nlod_training_step_noalloc(None, None, 100, None, None, None),
         "nlod_forward": lambda: L.nlod_forward(None, None, 128, None, None, None),
         "nlod_optimizer_step": lambda: L.nlod_optimizer_step(None, None),
         "nlod_autotune": lambda: L.nlod_autotune(None, None, 128, None, None),

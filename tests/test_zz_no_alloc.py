@@ -4,6 +4,11 @@ FP32 step whatever precision the module was created with, so it must give the sa
 nlod_training_step on the module's FP32 form, call after call, from its fixed scratch instead of a
 cudaMalloc'ed workspace.  Both entry points are called through the C ABI.
 
+The first call in a device's context is the set-up call (under lazy module loading it loads the
+scratch array and the step's kernels); the no-allocation check applies from the second call on.
+It reads the device-wide free memory, so it assumes that no other process allocates on this GPU
+while the test runs (the GPU is leased to this test run alone).
+
 This file is named so that pytest collects it last."""
 import ctypes as C
 
@@ -45,8 +50,8 @@ def test_training_step_noalloc_matches_training_step(cuda, nlod_lib, precision):
         assert nlod_lib.nlod_training_step_noalloc(noa.handle, stream, n, xd.data_ptr(), td.data_ptr(), loss_noa.data_ptr()) == 0, \
             nlod_lib.nlod_last_error()
         torch.cuda.synchronize()
-        if call == 1:
-            assert torch.cuda.mem_get_info()[0] == free_before   # nothing allocated by the call
+        if call >= 1:   # after the set-up call: nothing allocated by the call
+            assert torch.cuda.mem_get_info()[0] == free_before
         assert loss_noa.item() == pytest.approx(loss_ref.item(), rel=1e-5)
         g_ref, g_noa = ref.get_params("gradients"), noa.get_params("gradients")
         assert _rel(g_noa, g_ref) <= 1e-3
@@ -69,4 +74,6 @@ def test_training_step_noalloc_rejects_batches_beyond_its_scratch(cuda, nlod_lib
     assert code == 1
     msg = nlod_lib.nlod_last_error().decode()
     assert "16 MiB" in msg and "10880" in msg
+    # a batch that is not a multiple of 128 is rejected too, before any launch
+    assert nlod_lib.nlod_training_step_noalloc(m.handle, None, 100, x.data_ptr(), t.data_ptr(), None) == 1
     assert m.optimizer_step_count == 0
