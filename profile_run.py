@@ -1,10 +1,10 @@
 """Small, self-contained runs of single kernels of the hot path, for ncu captures.
 
-    python -m neural_lod_gb300.profile_run query  [--precision fp16] [--n 2097152] [--iters 3]
-    python -m neural_lod_gb300.profile_run train  [--precision fp16] [--n 262144]  [--iters 3]
-    python -m neural_lod_gb300.profile_run render [--precision fp16] [--iters 3]
-    python -m neural_lod_gb300.profile_run voxelize [--iters 3]
-    python -m neural_lod_gb300.profile_run sampler  [--iters 3]
+    python profile_run.py query  [--precision fp16] [--n 2097152] [--iters 3]
+    python profile_run.py train  [--precision fp16] [--n 262144]  [--iters 3]
+    python profile_run.py render [--precision fp16] [--iters 3]
+    python profile_run.py voxelize [--iters 3]
+    python profile_run.py sampler  [--iters 3]
 
 `query` runs the throughput-query forward (the bench's headline kernel) `iters` times on the
 bench's inputs; `train` runs visibility training steps.  Each run ends with a status check, so a
@@ -16,7 +16,7 @@ import argparse
 import sys
 from pathlib import Path
 
-sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+sys.path.insert(0, str(Path(__file__).resolve().parent))
 
 
 def main():

@@ -3,16 +3,19 @@ polynomials of the reference's own SH encoding (rptr/ext/tiny-cuda-nn/include/ti
 encodings/spherical_harmonics.h, kernel_sh: the `data_out(k) = ...;` lines), evaluated in float64
 at seeded directions.  Run where the reference sources are present:
 
-    python tests/golden/make_sh_golden.py [/path/to/reference]
+    python tests/golden/make_sh_golden.py <reference checkout>     # or NLOD_REFERENCE=<dir>
 """
+import os
 import re
 import sys
 from pathlib import Path
 
 import numpy as np
 
-ROOT = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
-SRC = ROOT / "rptr/ext/tiny-cuda-nn/include/tiny-cuda-nn/encodings/spherical_harmonics.h"
+_ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NLOD_REFERENCE")
+if not _ref:
+    raise SystemExit("give the reference checkout as the argument (or set NLOD_REFERENCE)")
+SRC = Path(_ref) / "rptr/ext/tiny-cuda-nn/include/tiny-cuda-nn/encodings/spherical_harmonics.h"
 
 
 def reference_polynomials():
@@ -41,7 +44,7 @@ def main():
     for k, expr in polys.items():
         vals[:, k] = np.broadcast_to(eval(expr, {"__builtins__": {}}, env), d.shape[0])
     out = Path(__file__).resolve().parent / "sh_golden.npz"
-    np.savez_compressed(out, dirs=d, values=vals, source=str(SRC.relative_to(ROOT)))
+    np.savez_compressed(out, dirs=d, values=vals, source=str(SRC.relative_to(Path(_ref))))
     print(out, vals.shape)
 
 

@@ -1,6 +1,6 @@
 """The throughput network shipped with the reference's arcade scene runs through the module:
-its restated configuration matches the shipped JSON's layout (CPU, when the reference tree is
-present), and on the GPU its FP32 and FP16 inference agree with the FP64 oracle, it trains, and a
+its restated configuration matches the shipped JSON's layout (CPU, when the reference's files are
+staged), and on the GPU its FP32 and FP16 inference agree with the FP64 oracle, it trains, and a
 checkpoint round trip reproduces it."""
 import json
 
@@ -9,16 +9,14 @@ import pytest
 
 import oracle
 from neural_lod_gb300 import workloads as W
-from oracle.build_ref import REFERENCE
-
-SHIPPED = REFERENCE / "neural_lod/scenes/arcade/learned_weights/arcade_world_final_512_throughput_config.json"
+from oracle.build_ref import ARCADE_CONFIG as SHIPPED   # the shipped JSON, staged from the reference
 
 
 def test_restated_config_matches_shipped_json():
     import neural_lod_gb300 as N
 
     if not SHIPPED.exists():
-        pytest.skip("reference tree not present")
+        pytest.skip("the shipped configuration is not staged (python -m oracle.build_ref stage)")
     cfg = json.loads(SHIPPED.read_text())
     enc, net, loss, opt = W.arcade_throughput_configs()
     assert N.layout(cfg["encoding"], cfg["network"], 9, 3) == N.layout(enc, net, 9, 3)
