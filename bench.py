@@ -179,6 +179,120 @@ def cpu_baseline(enc, net, n_in, n_out, params, x_all, target_cpu_seconds=12.0):
             "sample": f"first {n} queries of the throughput_query batch (same inputs and weights), FP32 scalar, {threads} threads"}
 
 
+def tcnn_comparison(dev, flush, args):
+    """tiny-cuda-nn, built from the reference's vendored sources (oracle/build_tcnn.py), on the same
+    GPU, workloads and timing as this library's legs: FP16 fully fused MLP + grid encoding, weights
+    injected from the same FP32 vectors.  tiny-cuda-nn has no one-hot encoding, so the throughput
+    network takes the LoD as 8 identity inputs (17 inputs, the same 72 encoded columns); this
+    library is timed on that same form beside it.  Returns None when the build is absent."""
+    import torch
+
+    from oracle import tcnn as T
+    if not T.available():
+        return None
+    # a non-default stream, so tiny-cuda-nn's trainer captures its forward + backward in a CUDA
+    # graph as it does in the application (trainer.h:175-180); both libraries run on it
+    with torch.cuda.stream(torch.cuda.Stream(dev)):
+        return _tcnn_comparison(dev, flush, args, T)
+
+
+def _tcnn_comparison(dev, flush, args, T):
+    import numpy as np
+    import torch
+
+    import oracle
+    from neural_lod_gb300 import NetworkWithInputEncoding, layout, workloads as W
+
+    res = {"live": True, "build": "rptr/ext/tiny-cuda-nn, 11 units + oracle/tcnn_harness.cu, nvcc -O3 sm_103a, TCNN_MIN_GPU_ARCH=103"}
+    steps = max(3, args.steps // 2)
+
+    # throughput query, 2^21, 17-input identity form
+    n = W.WORKLOADS["throughput_query"]["batch"]
+    enc, net = W.thr_identity_configs()
+    spec = layout(enc, net, 17, 3)
+    params = W.xavier_params(spec, seed=7)
+    xh = W.thr_identity_inputs(n, seed=1)
+    x = torch.from_numpy(xh).to(dev)
+    out = torch.empty((n, 3), device=dev)
+    tm = T.TcnnModel(17, 3, enc, net)
+    tm.set_params(params)
+    t_tc = statistics.mean(time_steps(lambda: tm.inference(x, out), steps, 3, flush))
+    ref = oracle.Oracle(enc, net, 17, 3).forward(xh[:4096], params)
+    err_tc = float(np.abs(tm.inference(x[:4096]).cpu().numpy() - ref).mean())
+    del tm
+    mo = NetworkWithInputEncoding(17, 3, enc, net, precision="fp16")
+    mo.set_params(params)
+    mo.autotune(x, out)
+    t_ours = statistics.mean(time_steps(lambda: mo.inference(x, out), steps, 3, flush))
+    err_ours = float(np.abs(mo.inference(x[:4096]).cpu().numpy() - ref).mean())
+    del mo
+    res["throughput_query"] = {"batch": n, "tcnn_queries_per_s": n / (t_tc * 1e-3), "ours_queries_per_s": n / (t_ours * 1e-3),
+                               "ours_over_tcnn": t_tc / t_ours, "tcnn_err_vs_fp64_mean_abs": err_tc,
+                               "ours_err_vs_fp64_mean_abs": err_ours}
+
+    # visibility query, 65,536, per-element max level
+    nv = W.WORKLOADS["visibility_query"]["batch"]
+    venc, vnet = W.visibility_configs()
+    vparams = W.xavier_params(layout(venc, vnet, 6, 1), seed=8)
+    xv, _, frac = W.visibility_inputs(nv, seed=2)
+    xvd, fd = torch.from_numpy(xv).to(dev), torch.from_numpy(frac).to(dev)
+    ov = torch.empty((nv, 1), device=dev)
+    tm = T.TcnnModel(6, 1, venc, vnet)
+    tm.set_params(vparams)
+    tm.set_max_level_gpu(fd)
+    t_tc = statistics.mean(time_steps(lambda: tm.inference(xvd, ov), args.steps, 3, flush))
+    del tm
+    mo = NetworkWithInputEncoding(6, 1, venc, vnet, precision="fp16")
+    mo.set_params(vparams)
+    mo.set_max_level_gpu(fd)
+    t_ours = statistics.mean(time_steps(lambda: mo.inference(xvd, ov), args.steps, 3, flush))
+    del mo
+    res["visibility_query"] = {"batch": nv, "tcnn_queries_per_s": nv / (t_tc * 1e-3), "ours_queries_per_s": nv / (t_ours * 1e-3),
+                               "ours_over_tcnn": t_tc / t_ours}
+
+    # training steps: visibility 2^18 (BCE, Adam) and throughput 2^20 (RelativeL2, EMA of decay of Adam)
+    def train_pair(enc_, net_, n_in, n_out, loss, opt, xt, tt, seed):
+        pr = W.xavier_params(layout(enc_, net_, n_in, n_out), seed=seed)
+        xd_, td_ = torch.from_numpy(xt).to(dev), torch.from_numpy(tt).to(dev)
+        tm_ = T.TcnnModel(n_in, n_out, enc_, net_, loss, opt)
+        tm_.set_params(pr)
+        t1 = statistics.mean(time_steps(lambda: tm_.training_step(xd_, td_), steps, 3, flush))
+        del tm_
+        mo_ = NetworkWithInputEncoding(n_in, n_out, enc_, net_, loss=loss, optimizer=opt, precision="fp16")
+        mo_.set_params(pr)
+        lo = torch.empty(1, device=dev)
+        t2 = statistics.mean(time_steps(lambda: mo_.training_step(xd_, td_, lo), steps, 3, flush))
+        del mo_
+        nb = xt.shape[0]
+        return {"batch": nb, "tcnn_samples_per_s": nb / (t1 * 1e-3), "ours_samples_per_s": nb / (t2 * 1e-3),
+                "ours_over_tcnn": t1 / t2}
+
+    nt = W.WORKLOADS["visibility_train"]["batch"]
+    tenc, tnet = W.visibility_configs(16)
+    xt, _, _ = W.visibility_inputs(nt, seed=3, n_grid_levels=16)
+    tt = (np.random.default_rng(3).random((nt, 1)) < 0.5).astype(np.float32)
+    res["visibility_train"] = train_pair(tenc, tnet, 6, 1, W.VISIBILITY_LOSS, W.VISIBILITY_OPTIMIZER, xt, tt, 9)
+    ntt = 1 << 20
+    res["throughput_train"] = train_pair(enc, net, 17, 3, W.THROUGHPUT_LOSS, W.THROUGHPUT_OPTIMIZER,
+                                         W.thr_identity_inputs(ntt, seed=4), W.rgb_targets(ntt, 4), 10)
+    return res
+
+
+def committed_tcnn_figures():
+    """The tiny-cuda-nn comparison measured earlier on this GPU model (profiles/tcnn_comparison.md,
+    its JSON block), for runs where oracle/_ref holds no tiny-cuda-nn build."""
+    p = ROOT / "profiles" / "tcnn_comparison.md"
+    reason = "tiny-cuda-nn is not built here (python -m oracle.build_tcnn build; about 10 minutes of nvcc)"
+    if not p.exists():
+        return {"live": False, "reason": reason}
+    text = p.read_text()
+    try:
+        block = text.split("```json", 1)[1].split("```", 1)[0]
+        return {"live": False, "reason": reason, "source": "profiles/tcnn_comparison.md", **json.loads(block)}
+    except (IndexError, ValueError):
+        return {"live": False, "reason": reason}
+
+
 def run_reference(args, world, rank):
     """Reference arm: the reference's CPU implementation of the path.  tiny-cuda-nn has no CPU
     path, so this times the FP32 restatement of its encoding + MLP (oracle port) on the host
@@ -482,6 +596,11 @@ def main():
                  "cpu_sample": "2^14 visibility samples + targets, host restatement, one thread"}
     del gsp, pyr
 
+    # ---- tiny-cuda-nn built from the reference's sources, same GPU and workloads ----
+    tcnn = tcnn_comparison(dev, flush, args) if rank == 0 else None
+    if tcnn is None:
+        tcnn = committed_tcnn_figures()
+
     # ---- aggregate over ranks ----
     total_queries = n * world
     t_step = ms16
@@ -535,6 +654,7 @@ def main():
         "voxelize_train": {"pyramid_ms": t_pyr * 1e3, "batch": n4, "batches": n_batches, **e2e4,
                            "targets": "albedo(voxel centre) x exact-DDA transmittance along wi, LoD 0-7 of the 1024^3 pyramid",
                            "loss": "RelativeL2", "optimizer": "Ema(0.95) of ExponentialDecay(Adam lr 5e-3)"},
+        "tcnn": tcnn,
         "clocks": clocks,
         "gpu_launches": len(times16),
         "kernel_variant": variant,

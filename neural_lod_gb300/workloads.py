@@ -152,6 +152,34 @@ def throughput_inputs(n: int, seed: int = 1):
     return x.astype(np.float32)
 
 
+def thr_identity_configs():
+    """The throughput network with the LoD one-hot given as 8 identity inputs (17 inputs: position,
+    wi, wo, one-hot).  The encoded input is the same 72 columns as throughput_configs(); this is the
+    form tiny-cuda-nn can build, since it has no one-hot encoding."""
+    enc, net = throughput_configs()
+    enc = {"otype": "Composite", "nested": enc["nested"][:3] + [{"otype": "Identity", "n_dims_to_encode": 8}]}
+    return enc, net
+
+
+def thr_identity_inputs(n: int, seed: int = 1) -> np.ndarray:
+    """throughput_inputs(n, seed) with the LoD column expanded to its one-hot row: float32 [n, 17]."""
+    x = throughput_inputs(n, seed=seed)
+    lod = np.floor(x[:, 9] * 8).astype(np.int64)
+    onehot = np.zeros((n, 8), np.float32)
+    onehot[np.arange(n), lod] = 1.0
+    return np.concatenate([x[:, :9], onehot], axis=1).astype(np.float32)
+
+
+def binary_targets(n: int, seed: int) -> np.ndarray:
+    """Seeded 0/1 visibility targets, float32 [n, 1]."""
+    return (np.random.default_rng(seed).random((n, 1)) < 0.5).astype(np.float32)
+
+
+def rgb_targets(n: int, seed: int) -> np.ndarray:
+    """Seeded RGB throughput targets U[0.05, 1], float32 [n, 3]."""
+    return np.random.default_rng(seed).uniform(0.05, 1.0, (n, 3)).astype(np.float32)
+
+
 def xavier_params(spec: dict, seed: int = 7) -> np.ndarray:
     """FP32 parameter vector for a layout spec: Xavier-uniform matrices (gpu_matrix.h:291-306),
     grid entries U[-1e-4, 1e-4] (grid.h:1353-1356), scaled up by `grid_gain` for test signal."""
