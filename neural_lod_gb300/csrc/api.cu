@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <functional>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -69,6 +70,7 @@ struct nlod_module {
     void* w_op = nullptr;           // operand copy (FP16/BF16) of the network part of `params`
     void* w_op_inf = nullptr;       // operand copy of the inference network weights
     uint16_t* grid_h = nullptr;     // FP16 copy of the inference parameters (grid part used), FP16 modules with grids
+    uint16_t* grid_h_train = nullptr;  // FP16 copy of the training values (grid part), FP16 modules with grids and an EMA
     uint32_t* status = nullptr;     // device status word (bounded-wait timeouts)
 
     const float* max_level_gpu = nullptr;
@@ -88,6 +90,9 @@ struct nlod_module {
     size_t enc_tiles_bytes = 0;
     uint8_t* host_io = nullptr;     // device outputs (and staged pageable inputs) of nlod_inference_host
     size_t host_io_bytes = 0;
+    // executable graphs of the fused training step, per kind (optimizer step yes/no x loss output yes/no)
+    cudaGraphExec_t step_graph[4] = {};
+    bool step_graph_warm = false;
 
     const float* inference_params() const { return ema ? ema : params; }
     int op_kind() const { return precision == NLOD_PRECISION_FP16 ? 1 : 2; }
@@ -139,6 +144,8 @@ void refresh_operand_copies(nlod_module* m, cudaStream_t s) {
         // the current values
         const uint32_t off = m->d.n_params_network, n = (uint32_t)(m->d.n_params - m->d.n_params_network);
         cuda_check(launch_convert_weights(m->inference_params() + off, m->grid_h + off, n, 1, s), "convert grid tables");
+        if (m->grid_h_train)
+            cuda_check(launch_convert_weights(m->params + off, m->grid_h_train + off, n, 1, s), "convert grid tables");
     }
 }
 
@@ -244,6 +251,7 @@ void run_optimizer(nlod_module* m, cudaStream_t s) {
     }
     // the same pass refreshes every derived copy: operand-type weights and the FP16 grid tables
     a.grid_h = reinterpret_cast<__half*>(m->grid_h);
+    a.grid_h_train = reinterpret_cast<__half*>(m->grid_h_train);
     a.w_op = m->precision == NLOD_PRECISION_FP32 ? nullptr : m->w_op;
     a.w_op_inf = m->precision == NLOD_PRECISION_FP32 ? nullptr : m->w_op_inf;
     a.op_kind = m->op_kind();
@@ -343,7 +351,10 @@ int nlod_module_create(const char* encoding_json, const char* network_json, cons
                 m->w_op = dev_alloc<uint16_t>(m->d.n_params_network);
                 m->w_op_inf = m->ema ? dev_alloc<uint16_t>(m->d.n_params_network) : m->w_op;
             }
-            if (precision == NLOD_PRECISION_FP16 && m->d.n_grids > 0) m->grid_h = dev_alloc<uint16_t>(np);
+            if (precision == NLOD_PRECISION_FP16 && m->d.n_grids > 0) {
+                m->grid_h = dev_alloc<uint16_t>(np);
+                if (m->ema) m->grid_h_train = dev_alloc<uint16_t>(np);
+            }
             init_params(m.get(), seed);
             refresh_operand_copies(m.get(), 0);
             cuda_check(cudaDeviceSynchronize(), "init");
@@ -441,11 +452,14 @@ void nlod_module_destroy(nlod_module* m) {
     dev_free(m->ema);
     if (m->w_op_inf != m->w_op) dev_free(m->w_op_inf);
     dev_free(m->grid_h);
+    dev_free(m->grid_h_train);
     dev_free(m->w_op);
     dev_free(m->status);
     dev_free(m->loss_partial);
     dev_free(m->enc_tiles);
     dev_free(m->host_io);
+    for (cudaGraphExec_t& g : m->step_graph)
+        if (g) cudaGraphExecDestroy(g);
     delete m;
 }
 
@@ -578,6 +592,48 @@ void nlod_ctx_destroy(nlod_ctx* ctx) {
     delete ctx;
 }
 
+// Runs the launches `issue` makes on s as one CUDA graph, as tiny-cuda-nn's Trainer does for its
+// step (trainer.h:175-180), here including the optimizer: the launches are captured on s, the
+// module's executable graph for this kind of step is updated in place with the new arguments
+// (cudaGraphExecUpdate; instantiated again only when the update is refused), and launched.  The
+// programmatic (PDL) edge between the encoding and the fused kernel is kept by the capture.
+// The module's first step, a step on the legacy default stream (which cannot be captured) and a
+// step on a stream the caller is capturing issue the launches directly.
+static void launch_step_graph(nlod_module* m, cudaStream_t s, int kind, const std::function<void(cudaStream_t)>& issue) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const bool capturable = m->step_graph_warm && s != nullptr && s != cudaStreamLegacy &&
+                            cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone;
+    if (!capturable) {
+        issue(s);
+        m->step_graph_warm = true;   // kernel attributes and buffers are set up by the direct launches
+        return;
+    }
+    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin step capture");
+    cudaGraph_t g = nullptr;
+    try {
+        issue(s);
+    } catch (...) {
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    cuda_check(cudaStreamEndCapture(s, &g), "end step capture");
+    cudaGraphExec_t& exec = m->step_graph[kind & 3];
+    if (exec) {
+        cudaGraphExecUpdateResultInfo info{};
+        if (cudaGraphExecUpdate(exec, g, &info) != cudaSuccess) {
+            (void)cudaGetLastError();
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    if (!exec) e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    cuda_check(e, "instantiate step graph");
+    cuda_check(cudaGraphLaunch(exec, s), "launch step graph");
+}
+
 static int train_impl(nlod_module* m, void* stream, uint32_t n, const float* in, const float* target, float* loss_out, bool run_opt) {
     return guarded([&] {
         if (!m) throw Error(NLOD_ERR_INVALID, "module is NULL");
@@ -604,12 +660,10 @@ static int train_impl(nlod_module* m, void* stream, uint32_t n, const float* in,
             t.grad_scale = loss_scale * t.inv_n_total;
             t.grads = m->grads;
             t.loss_partial = m->loss_partial;
-            // the FP16 grid copy holds the inference values: the training values only without an EMA
-            t.grid_h = m->ema ? nullptr : m->grid_h;
+            // FP16 training values: the inference copy without an EMA, the separate training copy with one
+            t.grid_h = m->ema ? m->grid_h_train : m->grid_h;
             // the encoding kernel zeroes the gradients (4-float tail, if any, by a memset)
             t.zero_grads_n = (uint32_t)(m->n_params & ~size_t(3));
-            if (t.zero_grads_n != m->n_params)
-                cuda_check(cudaMemsetAsync(m->grads + t.zero_grads_n, 0, sizeof(float) * (m->n_params - t.zero_grads_n), s), "memset grads");
             const size_t enc_bytes = (size_t)n * m->d.enc_width * 2u;
             if (m->enc_tiles_bytes < enc_bytes) {
                 dev_free(m->enc_tiles);
@@ -619,12 +673,19 @@ static int train_impl(nlod_module* m, void* stream, uint32_t n, const float* in,
                 m->enc_tiles_bytes = enc_bytes;
             }
             t.enc_tiles = m->enc_tiles;
-            cuda_check(launch_encode_tiles(m->d, t, m->op_kind(), s), "encoding");
-            cuda_check(launch_train_tc(m->d, t, m->op_kind(), m->train_groups, m->status, s), "training step");
-            // every CTA of the fused kernel wrote its partial: no memset, sum exactly those
-            if (loss_out) cuda_check(launch_reduce_sum(m->loss_partial, train_tc_blocks(n, m->train_groups), loss_out, 1.0f, s), "loss");
-            m->grad_scale = loss_scale;
-            if (run_opt) run_optimizer(m, s);
+            const auto issue = [&](cudaStream_t st) {
+                if (t.zero_grads_n != m->n_params)
+                    cuda_check(cudaMemsetAsync(m->grads + t.zero_grads_n, 0, sizeof(float) * (m->n_params - t.zero_grads_n), st),
+                               "memset grads");
+                cuda_check(launch_encode_tiles(m->d, t, m->op_kind(), st), "encoding");
+                cuda_check(launch_train_tc(m->d, t, m->op_kind(), m->train_groups, m->status, st), "training step");
+                // every CTA of the fused kernel wrote its partial: no memset, sum exactly those
+                if (loss_out)
+                    cuda_check(launch_reduce_sum(m->loss_partial, train_tc_blocks(n, m->train_groups), loss_out, 1.0f, st), "loss");
+                m->grad_scale = loss_scale;
+                if (run_opt) run_optimizer(m, st);
+            };
+            launch_step_graph(m, s, (run_opt ? 2 : 0) | (loss_out ? 1 : 0), issue);
             return;
         }
         ensure_workspace(m, n);

@@ -132,6 +132,9 @@ struct AdamStepArgs {
     // nullable: FP16 copy of the inference values (the EMA when present) of the non-matrix
     // parameters, refreshed in the same pass
     __half* grid_h;
+    // nullable: FP16 copy of the training values of the non-matrix parameters, kept apart from
+    // grid_h when an EMA makes the inference values differ (the FP16 training step gathers from it)
+    __half* grid_h_train;
     // nullable: operand-type copies of the matrix parameters (training values, inference values),
     // refreshed in the same pass; op_kind 1 = FP16, 2 = BF16
     void* w_op;

@@ -1,0 +1,118 @@
+"""Accuracy of the training-step gradients at a trained (non-degenerate) point of the visibility
+training workload: batch 2^18, 16-level grid + SH 4 -> 64 -> 64 -> 1 sigmoid, BCE, Adam lr 1e-2
+(beta 0.9 / 0.99, eps 1e-15), binary transmittance targets by exact DDA through a seeded 256^3
+value-noise occupancy (30 % occupied).
+
+The module first takes 100 Adam steps from the seeded start, so that the gradient is not the
+heavily cancelling one of a random start.  At that point the gradients of one step (no optimizer)
+of the FP16 and BF16 tensor-core forms and of the plain FP32 form are compared, per parameter
+block, with the FP64 oracle's analytic gradient, which is itself checked against FP64 central
+differences (h = 1e-4) on sampled parameters.  Also reported: the relative error over 1,024
+sampled parameters with a nonzero gradient.
+
+Bounds (relative L2 error per block):  FP32 form 1e-4;  FP16 and BF16 forms as stated in
+FP16_BOUND / BF16_BOUND below, from the measurement printed by this test.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from neural_lod_gb300 import NetworkWithInputEncoding, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+N = 1 << 18
+FP16_BOUND = 1e-2
+BF16_BOUND = 8e-2
+FP32_BOUND = 1e-4
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def trained(cuda, nlod_lib):
+    import torch
+
+    from neural_lod_gb300 import samples as S
+    from neural_lod_gb300.lod import LodGrid
+
+    noise = W.value_noise_occupancy(256, seed=5, spacing=16, density=0.3)
+    grid = LodGrid(W.pack_bits(noise), 256, 8)
+    x, _, t = S.visibility_batch(grid, N, seed=3)
+    del grid
+    enc, net = W.visibility_configs(16)
+    spec = oracle.model_spec(enc, net, 6, 1)
+    params0 = W.xavier_params(spec, seed=9)
+    xd, td = torch.from_numpy(x).to(cuda), torch.from_numpy(t).to(cuda)
+    m = NetworkWithInputEncoding(6, 1, enc, net, loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER, precision="fp16")
+    m.set_params(params0)
+    first = m.training_step(xd, td).item()
+    for _ in range(99):
+        last = m.training_step(xd, td)
+    m.sync_status()
+    print(f"\nBCE loss: step 1 {first:.5f}, step 100 {last.item():.5f}")
+    p = m.get_params("params").astype(np.float32)
+    orc = oracle.Oracle(enc, net, 6, 1)
+    loss64, g64 = orc.loss_and_grad("BinaryCrossEntropy", x, p.astype(np.float64), t)
+    return dict(x=x, t=t, xd=xd, td=td, enc=enc, net=net, spec=spec, p=p, orc=orc, loss64=loss64, g64=g64)
+
+
+def test_oracle_gradient_is_central_differences_at_the_trained_point(trained):
+    """The FP64 analytic gradient against FP64 central differences (h = 1e-4) of the full-batch
+    loss, on MLP weights and touched grid entries."""
+    orc, x, t, g = trained["orc"], trained["x"], trained["t"], trained["g64"]
+    p = trained["p"].astype(np.float64)
+    n_net = trained["spec"]["n_params_network"]
+    rng = np.random.default_rng(7)
+    net_idx = rng.choice(np.nonzero(g[:n_net])[0], 6, replace=False)
+    grid_idx = rng.choice(n_net + np.nonzero(g[n_net:])[0], 10, replace=False)
+
+    def loss(q):
+        _, y16 = orc.forward(x, q, with_y16=True)
+        return orc.loss("BinaryCrossEntropy", y16, t)[0]
+
+    h = 1e-4
+    errs = []
+    for i in np.concatenate([net_idx, grid_idx]):
+        q = p.copy()
+        q[i] += h
+        fp = loss(q)
+        q[i] -= 2 * h
+        fm = loss(q)
+        fd = (fp - fm) / (2 * h)
+        errs.append(abs(fd - g[i]) / max(abs(g[i]), 1e-9))
+    print(f"\noracle gradient vs central differences: median rel {np.median(errs):.1e}, max {np.max(errs):.1e}")
+    # a ReLU kink of a few of the 2^18 samples inside +-h moves a difference quotient slightly
+    assert np.median(errs) <= 1e-5
+    assert np.max(errs) <= 1e-3
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16", "fp32"])
+def test_gradient_accuracy_at_trained_point(trained, precision):
+    spec, p, g64 = trained["spec"], trained["p"], trained["g64"]
+    m = NetworkWithInputEncoding(6, 1, trained["enc"], trained["net"], loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER,
+                                 precision=precision)
+    m.set_params(p)
+    loss = m.training_step(trained["xd"], trained["td"], run_optimizer=False).item()
+    m.sync_status()
+    g = m.get_params("gradients").astype(np.float64)
+    blocks = {}
+    for k, L in enumerate(spec["layers"]):
+        sl = slice(L["offset"], L["offset"] + L["in"] * L["out"])
+        blocks[f"W{k} {L['in']}x{L['out']}"] = _rel(g[sl], g64[sl])
+    n_net = spec["n_params_network"]
+    blocks["grid"] = _rel(g[n_net:], g64[n_net:])
+    nz = np.nonzero(g64)[0]
+    idx = np.random.default_rng(11).choice(nz, 1024, replace=False)
+    sampled = _rel(g[idx], g64[idx])
+    loss_err = abs(loss - trained["loss64"]) / trained["loss64"]
+    print(f"\n{precision}: loss rel {loss_err:.2e}; 1,024 sampled params rel {sampled:.2e}; " +
+          "; ".join(f"{k} {v:.2e}" for k, v in blocks.items()))
+    bound = {"fp16": FP16_BOUND, "bf16": BF16_BOUND, "fp32": FP32_BOUND}[precision]
+    for k, v in blocks.items():
+        assert v <= bound, (precision, k, v)
+    assert sampled <= bound

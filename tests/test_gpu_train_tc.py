@@ -12,13 +12,16 @@ Two references:
     sums cancel heavily), not of the kernel;
   * a float64 model of the same computation with the kernel's roundings (weights, encoded
     features, activations, output gradients and deltas rounded to FP16 / BF16, and in the FP16
-    form without an EMA the grid tables too, which it gathers from their FP16 copy; everything
+    form the grid tables too, which it gathers from an FP16 copy of the training values (its own
+    copy when an EMA holds the inference values); everything
     else exact, products summed in float32): the network-weight gradients agree to about 1e-5
     relative, which pins the fused kernel's data flow.  The check allows 1e-2 (FP16) / 2e-2
     (BF16): a hidden pre-activation within rounding distance of zero can round to a different
     sign in a differently ordered sum, flipping one ReLU mask bit, and at these cancelling
     starting-point gradients one flipped bit moves a dW column by a few 1e-3.
 The FP32 form is held to 1e-3 against the FP64 oracle in test_gpu_training.py."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -105,7 +108,7 @@ def _check(m, orc, spec, params, x, t, loss_name, precision, cuda, ml=None, ema=
     untouched = ref_g[n_net:] == 0
     assert np.all(g[n_net:][untouched] == 0)
     # the same computation with the kernel's roundings, in float64
-    model = _rounding_model(orc, spec, params, x, t, loss_name, precision, ml, fp16_tables=precision == "fp16" and not ema)
+    model = _rounding_model(orc, spec, params, x, t, loss_name, precision, ml, fp16_tables=precision == "fp16")
     for L, gm in zip(spec["layers"], model):
         gl = g[L["offset"]:L["offset"] + L["in"] * L["out"]].reshape(L["out"], L["in"])
         e = _rel(gl, gm)
@@ -192,3 +195,40 @@ def test_identity_hidden_activation(cuda, nlod_lib, precision):
     x, _, _ = W.visibility_inputs(n, seed=16)
     t = (np.random.default_rng(6).random((n, 1)) < 0.4).astype(np.float32)
     _check(m, oracle.Oracle(enc, net, 6, 1), spec, params, x, t, "BinaryCrossEntropy", precision, cuda)
+
+
+@pytest.mark.parametrize("with_ema", [False, True])
+def test_training_step_graph_matches_direct_launches(cuda, nlod_lib, with_ema):
+    """On a non-default stream the fused step (encode, fused kernel, loss sum, Adam) runs as one
+    CUDA graph updated per call; on the legacy default stream it is launched directly.  Both give
+    the same bits, over steps that change the inputs, the batch size, the learning rate schedule
+    and whether a loss is returned."""
+    import torch
+
+    enc, net = W.throughput_configs()
+    spec = oracle.model_spec(enc, net, 10, 3)
+    params = W.test_params(spec, seed=8, grid_scale=0.2)
+    opt = W.THROUGHPUT_OPTIMIZER if with_ema else W.THROUGHPUT_OPTIMIZER["nested"]["nested"]
+    batches = []
+    for i, n in enumerate([4096, 4096, 2048, 4096, 8192]):
+        x = torch.from_numpy(W.throughput_inputs(n, seed=40 + i)).to(cuda)
+        t = torch.from_numpy(np.random.default_rng(40 + i).random((n, 3)).astype(np.float32)).to(cuda)
+        batches.append((x, t))
+    results = {}
+    for mode in ("direct", "graph"):
+        m = NetworkWithInputEncoding(10, 3, enc, net, loss=W.THROUGHPUT_LOSS, optimizer=opt, precision="fp16")
+        m.set_params(params)
+        stream = torch.cuda.Stream(cuda) if mode == "graph" else torch.cuda.default_stream(cuda)
+        losses = []
+        with torch.cuda.stream(stream):
+            sp = C.c_void_p(stream.cuda_stream or None)
+            for k, (x, t) in enumerate(batches * 2):
+                if k % 3 == 2:   # no loss output: another kind of step graph
+                    assert nlod_lib.nlod_training_step(m.handle, sp, x.shape[0], x.data_ptr(), t.data_ptr(), None) == 0
+                else:
+                    losses.append(m.training_step(x, t).clone())
+            torch.cuda.synchronize()
+        m.sync_status()
+        results[mode] = (m.get_params("params"), m.get_params("inference"), torch.stack(losses).cpu().numpy())
+    for a, b in zip(results["direct"], results["graph"]):
+        assert np.array_equal(a, b)

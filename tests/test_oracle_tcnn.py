@@ -15,7 +15,7 @@ FP16 rounding.  A misread of any semantic above shows up as an error of the orde
 themselves (1e-1 and more), far above these bounds:
   query outputs       mean |tcnn - fp64| <= 2e-3 * mean |fp64| + 2e-4 (with the max level, too)
   loss                |tcnn - fp64| <= 2e-3 * |fp64|
-  MLP gradients       relative L2 <= 2e-2
+  MLP gradients       relative L2 <= 3e-2
   grid gradients      relative L2 <= 6e-2 on a seeded sample of 8,192 entries
   params after Adam   the update's sign agrees on >= 99 % of the changed entries; entries with
                       a zero gradient are unchanged (Adam skips them, adam.h:76-79)
@@ -79,7 +79,7 @@ def test_oracle_matches_tcnn_visibility_gradients(gold):
     loss, g = orc.loss_and_grad("BinaryCrossEntropy", x, params, t)
     assert abs(float(gold[f"{name}/loss"]) - loss) <= 2e-3 * abs(loss)
     n_net = spec["n_params_network"]
-    assert _rel(gold[f"{name}/grad_net"], g[:n_net]) <= 2e-2
+    assert _rel(gold[f"{name}/grad_net"], g[:n_net]) <= 3e-2
     idx = gold[f"{name}/grid_idx"]
     assert _rel(gold[f"{name}/grad_grid"], g[idx]) <= 6e-2
 
