@@ -531,7 +531,9 @@ def main():
     rv_params = W.xavier_params(layout(venc, vnet, 6, 1), seed=12)
     rt_params = W.xavier_params(layout(henc, hnet, 10, 3), seed=13)
     render = {}
-    for prec in ("fp16", "fp32"):
+    from neural_lod_gb300.render import MODE_WAVEFRONT
+    for form in ("fp16", "fp16_wavefront", "fp32"):
+        prec = form.split("_")[0]
         rv = NetworkWithInputEncoding(6, 1, venc, vnet, precision=prec)
         rt = NetworkWithInputEncoding(10, 3, henc, hnet, precision=prec)
         rv.set_params(rv_params)
@@ -541,15 +543,16 @@ def main():
             rv.autotune(xa, torch.empty((1 << 18, 1), device=dev))
             xb = torch.from_numpy(W.throughput_inputs(1 << 18, seed=6)).to(dev)
             rt.autotune(xb, torch.empty((1 << 18, 3), device=dev))
-        rr = Renderer(rv, rt, pyr, rparams)
+        rr = Renderer(rv, rt, pyr, RenderParams(**{**rparams.__dict__, "mode": MODE_WAVEFRONT}) if "wavefront" in form else rparams)
         frame = torch.empty((1024, 1024, 3), device=dev)
         ft = time_steps(lambda: rr.frame(frame), max(5, args.steps) if prec != "fp32" else 5, 3, flush)
         q = rr.stats()
         ft_sorted = sorted(ft)
         p50 = ft_sorted[len(ft) // 2]
         p99 = ft_sorted[min(len(ft) - 1, int(round(0.99 * (len(ft) - 1))))]
-        render[prec] = {"p50_ms": p50, "p99_ms": p99, "frames": len(ft), "vis_queries": q[0], "thr_queries": q[1],
-                        "rounds": q[2], "dropped_rays": q[3], "queries_per_s": (q[0] + q[1]) / (statistics.mean(ft) * 1e-3)}
+        render[form] = {"p50_ms": p50, "p99_ms": p99, "frames": len(ft), "vis_queries": q[0], "thr_queries": q[1],
+                        "rounds": q[2], "dropped_rays": q[3], "queries_per_s": (q[0] + q[1]) / (statistics.mean(ft) * 1e-3),
+                        "form": "persistent kernel" if rr.mode == 2 else "wavefront rounds"}
         rr.close()
         del rv, rt
     # host restatement on a bounded sample of the same frame (FP64 networks, all host threads)
@@ -645,7 +648,8 @@ def main():
                              "speedup_fp16_vs_fp32": ttrain["fp32"] / ttrain["fp16"]},
         "render": {"workload": "1024x1024 pinhole rays, level 3 (64^3) of a 512^3->4^3 pyramid (256^3 value noise, "
                                "30% occupied, upsampled x2), 4 path vertices, <= 64 visibility queries per bounce",
-                   "frame": "one CUDA-graph launch (rounds in a conditional while node)", **render,
+                   "frame": "one CUDA-graph launch: the persistent kernel (fp16) or rounds in a conditional while node "
+                            "(fp16_wavefront, fp32)", **render,
                    "cpu_queries_per_s": (rtot[0] + rtot[1]) / cpu_render_s,
                    "cpu_sample": "96x96 rays of the same camera, FP64 host restatement, all host threads"},
         "sample_generator": generator,

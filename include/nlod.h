@@ -291,8 +291,11 @@ NLOD_API int nlod_voxelize(const float* triangles, uint64_t n_triangles, uint32_
  * any bounce) or throughput x environment radiance.  This is the reference's wavefront loop
  * (rptr/cuda/neural-lod/wavefront_neural_throughput_visibility_lod.cu:470-720 with the per-ray
  * steps of rptr/cuda/wavefront_neural_pt.cuh: raymarch_impl, generate_*_inference_data_impl,
- * check_visibility, process_ray_bounce) without the host round trip per wavefront: a frame is one
- * CUDA-graph launch whose rounds run in a conditional while node.
+ * check_visibility, process_ray_bounce) without the host round trip per wavefront.  A frame is one
+ * CUDA-graph launch, in one of two forms: the persistent form (tensor-core modules) is one kernel
+ * whose tile pipelines refill their ray slots from a queue and run both networks on full tiles;
+ * the wavefront form advances every ray one query per round, the rounds running in a conditional
+ * while node.  Both forms give the same pixels and query counts.
  * Network inputs: visibility = (voxel-local entry point in [0,1]^3, (dir + 1) / 2) with
  * lod_max_level as the grid's max level; throughput = (voxel centre / res, (wi + 1) / 2,
  * (wo + 1) / 2, lod_input), wo = -dir.  Camera and radiance parameters are the renderer's. */
@@ -310,23 +313,34 @@ typedef struct nlod_render_params {
     float lod_max_level;           /* visibility network's max grid level fraction for this LoD */
     float lod_input;               /* throughput network's LoD input column for this LoD */
     uint64_t seed;                 /* direction sampling */
+    uint32_t mode;                 /* NLOD_RENDER_AUTO: the persistent kernel when both modules are tensor-core
+                                      modules of one operand type, else the wavefront rounds;
+                                      NLOD_RENDER_WAVEFRONT / NLOD_RENDER_PERSISTENT force one form */
 } nlod_render_params;
+
+#define NLOD_RENDER_AUTO 0
+#define NLOD_RENDER_WAVEFRONT 1
+#define NLOD_RENDER_PERSISTENT 2
 
 /* Index-space camera of a level with res voxels per axis: eye[3], right[3] (scaled by
  * tan(fov/2) * aspect), up[3] (scaled by tan(fov/2)), forward[3].  Host only. */
 NLOD_API int nlod_render_camera(const nlod_render_params* p, uint32_t level_res, float* out12);
 /* Builds the frame graph (allocates the ray state and query buffers); the modules and the grid
- * must outlive the renderer.  Synchronous. */
+ * must outlive the renderer.  Synchronous.  NLOD_ERR_UNSUPPORTED when mode is
+ * NLOD_RENDER_PERSISTENT and the modules cannot run the persistent form. */
 NLOD_API int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const nlod_lod_grid* grid,
                                   const nlod_render_params* p, nlod_renderer** out);
 NLOD_API void nlod_renderer_destroy(nlod_renderer* r);
 /* Renders one frame: image [height][width][3] FP32 device (NULL to skip the copy), ray_stats
  * [height*width][2] visibility / throughput queries per ray (NULL to skip).  Asynchronous. */
 NLOD_API int nlod_render_frame(nlod_renderer* r, void* stream, float* image, uint32_t* ray_stats);
-/* Totals of the last frame: visibility queries, throughput queries, rounds, rays dropped at the
- * per-bounce cap.  Synchronises; NLOD_ERR_TIMEOUT if a ray ran out of DDA steps or the frame hit
- * its round bound. */
+/* Totals of the last frame: visibility queries, throughput queries, rounds (persistent form: the
+ * most tile iterations of one pipeline), rays dropped at the per-bounce cap.  Synchronises;
+ * NLOD_ERR_TIMEOUT if a ray ran out of DDA steps, the frame hit its round or time bound, or a
+ * tensor-core wait timed out. */
 NLOD_API int nlod_render_stats(nlod_renderer* r, void* stream, uint64_t* out4);
+/* The form the renderer runs: NLOD_RENDER_WAVEFRONT or NLOD_RENDER_PERSISTENT. */
+NLOD_API int nlod_renderer_mode(const nlod_renderer* r);
 
 /* ---- Per-voxel visibility thresholds ----------------------------------------------------------
  * optimise_thresholds_for_voxel_grid (rptr/cuda/neural-lod/neural_lod_learning.cu:122-293, metrics

@@ -78,6 +78,7 @@ SIGNATURES = [
     ("nlod_renderer_destroy", None, [_vp]),
     ("nlod_render_frame", C.c_int, [_vp, _vp, _fp, _fp]),
     ("nlod_render_stats", C.c_int, [_vp, _vp, _fp]),
+    ("nlod_renderer_mode", C.c_int, [_vp]),
     ("nlod_optimal_thresholds", C.c_int, [_fp, _fp, _u32, _u32, C.c_int, C.c_float, _fp, _vp]),
     ("nlod_morton_voxels", C.c_int, [_fp, _u32, _fp, _u32, _fp, _vp]),
     ("nlod_sample_visibility", C.c_int, [_vp, _fp, _fp, _u32, _u32, _fp, _fp, _fp, _vp]),

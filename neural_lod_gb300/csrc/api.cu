@@ -290,6 +290,20 @@ cudaError_t module_inference_device_count(nlod_module* m, uint32_t n_max, const 
 
 uint32_t* module_status_word(nlod_module* m) { return m->status; }
 
+// Inference operands of a tensor-core module for the persistent renderer: its description, the
+// inference weights in the operand type and the parameter vector its encoding gathers (FP16 copy
+// for the FP16 form, FP32 inference values for the BF16 form).  False for the plain FP32 form.
+bool module_tc_operands(nlod_module* m, const ModelDesc** d, const void** weights, const void** table, int* kind) {
+    if (!m || m->precision == NLOD_PRECISION_FP32) return false;
+    if (m->precision == NLOD_PRECISION_FP16 && m->d.n_grids > 0 && !m->grid_h) return false;
+    *d = &m->d;
+    *weights = m->w_op_inf;
+    *table = m->precision == NLOD_PRECISION_FP16 && m->grid_h ? static_cast<const void*>(m->grid_h)
+                                                             : static_cast<const void*>(m->inference_params());
+    *kind = m->op_kind();
+    return true;
+}
+
 }  // namespace nlod
 
 extern "C" {

@@ -35,6 +35,8 @@
 #include "lod.h"
 #include "lod_dda.cuh"
 #include "nlod.h"
+#include "render_common.cuh"
+#include "render_pk.h"
 
 struct nlod_module;
 
@@ -42,48 +44,11 @@ namespace nlod {
 
 cudaError_t module_inference_device_count(nlod_module* m, uint32_t n_max, const float* in, float* out, const uint32_t* n_dev,
                                           float max_level, cudaStream_t s);
+bool module_tc_operands(nlod_module* m, const ModelDesc** d, const void** weights, const void** table, int* kind);
 
 namespace {
 
-constexpr uint32_t kFull = 0xFFFFFFFFu;
-constexpr float kFourPi = 12.566370614359172f;
-
-// One ray's state between rounds (80 bytes).
-struct alignas(16) RayState {
-    float o[3];
-    float tmin;
-    float d[3];
-    float tnear;
-    float tp[3];
-    float tfar;
-    int32_t ijk[3];
-    uint32_t meta;     // bits 0-7 bounce, 8-23 visibility queries in this bounce
-    float wi[3];
-    uint32_t pad;
-};
-
-struct RenderConsts {
-    LodLevelDev L;
-    uint32_t width, height, n_rays;
-    float cam_o[3], cam_u[3], cam_v[3], cam_w[3];
-    uint32_t max_depth, max_vis;
-    float threshold;
-    float background[3], env[3];
-    float res;
-    float lod_input;
-    uint32_t seed_lo, seed_hi;
-    uint32_t budget;
-    uint32_t max_rounds;
-};
-
-// Control words: [0..3] list counters [parity * 2 + kind], [4] visibility rows, [5] throughput
-// rows of the current round, [6] round, [7] rays dropped at the per-bounce query cap;
-// then 64-bit totals: visibility queries, throughput queries, rounds.
-struct Control {
-    uint32_t cnt[4];
-    uint32_t n_vis, n_thr, round, dropped;
-    unsigned long long tot_vis, tot_thr, tot_rounds, pad;
-};
+using namespace render;
 
 struct RenderBufs {
     RayState* rays;
@@ -97,39 +62,6 @@ struct RenderBufs {
     uint32_t* ray_stats;  // [n_rays][2]
     uint32_t* status;
 };
-
-__device__ __forceinline__ uint32_t mix32(uint32_t h) {
-    h ^= h >> 16;
-    h *= 0x7feb352du;
-    h ^= h >> 15;
-    h *= 0x846ca68bu;
-    h ^= h >> 16;
-    return h;
-}
-
-__device__ __forceinline__ float u01(uint32_t h) { return (float)(h >> 8) * (1.0f / 16777216.0f); }
-
-// Uniform direction on the sphere by rejection from the cube (correctly rounded operations only,
-// so that the host restatement draws the identical direction).
-__device__ __forceinline__ void sample_sphere(uint32_t key, float (&w)[3]) {
-    for (uint32_t t = 0; t < 16; ++t) {
-        const uint32_t h = mix32(key + t * 0x632BE5ABu);
-        const float x = __fsub_rn(__fmul_rn(2.f, u01(h)), 1.f);
-        const float y = __fsub_rn(__fmul_rn(2.f, u01(mix32(h ^ 0x68E31DA4u))), 1.f);
-        const float z = __fsub_rn(__fmul_rn(2.f, u01(mix32(h ^ 0xB5297A4Du))), 1.f);
-        const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
-        if (r2 <= 1.f && r2 >= 1e-4f) {
-            const float r = __fsqrt_rn(r2);
-            w[0] = __fdiv_rn(x, r);
-            w[1] = __fdiv_rn(y, r);
-            w[2] = __fdiv_rn(z, r);
-            return;
-        }
-    }
-    w[0] = 0.f;
-    w[1] = 0.f;
-    w[2] = 1.f;
-}
 
 // Appends the lanes with `want` to a list; returns each wanting lane's slot.  All lanes call.
 __device__ __forceinline__ uint32_t push(uint32_t* counter, bool want) {
@@ -160,111 +92,41 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ RenderCons
             bool march = false;
             if (first) {
                 ray = j;
-                const uint32_t px = j % C.width, py = j / C.width;
-                const float W = (float)C.width, H = (float)C.height;
-                const float a = __fdiv_rn(__fsub_rn(__fmul_rn(2.f, __fadd_rn((float)px, 0.5f)), W), W);
-                const float b = __fdiv_rn(__fsub_rn(H, __fmul_rn(2.f, __fadd_rn((float)py, 0.5f))), H);
-                float dd[3];
+                ray_generate(C, j, st);
 #pragma unroll
-                for (int k = 0; k < 3; ++k) dd[k] = __fadd_rn(__fadd_rn(__fmul_rn(a, C.cam_u[k]), __fmul_rn(b, C.cam_v[k])), C.cam_w[k]);
-                const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dd[0], dd[0]), __fmul_rn(dd[1], dd[1])), __fmul_rn(dd[2], dd[2])));
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    st.o[k] = C.cam_o[k];
-                    st.d[k] = __fdiv_rn(dd[k], len);
-                    st.tp[k] = 1.f;
-                    st.ijk[k] = -1;
-                    st.wi[k] = 0.f;
-                    B.image[3 * ray + k] = 0.f;
-                }
-                st.tmin = 0.f;
-                st.tnear = st.tfar = 0.f;
-                st.meta = 0u;
-                st.pad = 0u;
+                for (int k = 0; k < 3; ++k) B.image[3 * ray + k] = 0.f;
                 B.ray_stats[2 * ray] = 0u;
                 B.ray_stats[2 * ray + 1] = 0u;
                 march = true;
             } else if (j < nv) {
                 ray = B.lists[(p * 2 + 0) * C.n_rays + j];
                 st = B.rays[ray];
-                const float v = B.vis_out[j];
-                if (v >= C.threshold) {
-                    const uint32_t bounce = st.meta & 0xFFu;
-                    if (bounce + 1 < C.max_depth) {
-                        sample_sphere(mix32(mix32(ray ^ mix32(C.seed_lo ^ mix32(C.seed_hi))) ^ (bounce * 0x9E3779B9u)), st.wi);
-                        act = ACT_THR;
-                    }
-                    // a hit on the last bounce ends the path without radiance
-                } else {
-                    st.tmin = __fmul_rn(__fadd_rn(st.tnear, st.tfar), 0.5f);
-                    march = true;
-                }
+                const int vr = vis_resolve(C, st, ray, B.vis_out[j]);
+                if (vr == VIS_ACCEPT_THR) act = ACT_THR;
+                march = vr == VIS_REJECT;
             } else {
                 const uint32_t jj = j - nv;
                 ray = B.lists[(p * 2 + 1) * C.n_rays + jj];
                 st = B.rays[ray];
-                const float t_eps = __fadd_rn(st.tnear, __fmul_rn(1e-4f, __fsub_rn(st.tfar, st.tnear)));
-                bool alive = false;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const float tv = fmaxf(B.thr_out[3 * jj + k], 0.f);
-                    st.tp[k] = __fmul_rn(st.tp[k], __fmul_rn(tv, kFourPi));
-                    alive |= st.tp[k] != 0.f;
-                    st.o[k] = __fadd_rn(st.o[k], __fmul_rn(st.d[k], t_eps));
-                    st.d[k] = st.wi[k];
-                }
-                st.tmin = 0.f;
-                st.meta = (st.meta & 0xFFu) + 1u;   // next bounce, no visibility query yet
-                march = alive;
+                const float t[3] = {B.thr_out[3 * jj], B.thr_out[3 * jj + 1], B.thr_out[3 * jj + 2]};
+                march = thr_resolve(st, t);
             }
             if (march) {
-                const uint32_t nvis = (st.meta >> 8) & 0xFFFFu;
-                if (nvis >= C.max_vis) {
-                    atomicAdd(&B.ctl->dropped, 1u);
-                } else {
-                    int32_t v3[3] = {0, 0, 0};
-                    float tn = 0.f, tf = 0.f;
-                    const int r = dda::first_active_voxel(C.L, st.o, st.d, st.tmin, st.ijk, v3, tn, tf, C.budget);
-                    if (r < 0) {
-                        atomicOr(B.status, 2u);
-                    } else if (r == 0) {
-                        // escaped: background before the first bounce, environment after
-                        const uint32_t bounce = st.meta & 0xFFu;
-#pragma unroll
-                        for (int k = 0; k < 3; ++k) B.image[3 * ray + k] = bounce == 0 ? C.background[k] : __fmul_rn(st.tp[k], C.env[k]);
-                    } else {
-#pragma unroll
-                        for (int k = 0; k < 3; ++k) st.ijk[k] = v3[k];
-                        st.tnear = tn;
-                        st.tfar = tf;
-                        st.meta += 1u << 8;
-                        act = ACT_VIS;
-                    }
-                }
+                const int mr = ray_march(C, st, B.image + 3 * (size_t)ray);
+                if (mr == MARCH_DROPPED) atomicAdd(&B.ctl->dropped, 1u);
+                else if (mr == MARCH_FAIL) atomicOr(B.status, 2u);
+                else if (mr == MARCH_VIS) act = ACT_VIS;
             }
         }
         const uint32_t slot_v = push(&B.ctl->cnt[q * 2 + 0], act == ACT_VIS);
         const uint32_t slot_t = push(&B.ctl->cnt[q * 2 + 1], act == ACT_THR);
         if (act == ACT_VIS) {
             B.lists[(q * 2 + 0) * C.n_rays + slot_v] = ray;
-            float* row = B.vis_in + 6 * (size_t)slot_v;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const float pk = __fadd_rn(st.o[k], __fmul_rn(st.d[k], st.tnear));
-                row[k] = fminf(fmaxf(__fsub_rn(pk, (float)st.ijk[k]), 0.f), 1.f);
-                row[3 + k] = __fmul_rn(__fadd_rn(st.d[k], 1.f), 0.5f);
-            }
+            vis_row(st, B.vis_in + 6 * (size_t)slot_v);
             B.ray_stats[2 * ray] += 1u;
         } else if (act == ACT_THR) {
             B.lists[(q * 2 + 1) * C.n_rays + slot_t] = ray;
-            float* row = B.thr_in + 10 * (size_t)slot_t;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                row[k] = __fdiv_rn(__fadd_rn((float)st.ijk[k], 0.5f), C.res);
-                row[3 + k] = __fmul_rn(__fadd_rn(st.wi[k], 1.f), 0.5f);
-                row[6 + k] = __fmul_rn(__fadd_rn(-st.d[k], 1.f), 0.5f);
-            }
-            row[9] = C.lod_input;
+            thr_row(C, st, B.thr_in + 10 * (size_t)slot_t);
             B.ray_stats[2 * ray + 1] += 1u;
         }
         if (valid) B.rays[ray] = st;
@@ -308,6 +170,8 @@ struct nlod_renderer {
     RenderBufs B{};
     uint32_t n_pad = 0;
     float vis_max_level = 1000.f;
+    int mode = NLOD_RENDER_WAVEFRONT;
+    int pk_groups = 0;              // tile pipelines per CTA of the persistent form (autotuned)
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -415,6 +279,76 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             r->vis_max_level = p->lod_max_level;
             const uint32_t n = C.n_rays;
             r->n_pad = (n + 127u) / 128u * 128u;
+            // ---- the persistent form, when both modules are tensor-core modules of one type ----
+            const ModelDesc *dv = nullptr, *dt = nullptr;
+            PkArgs pk{};
+            int kv = 0, kt = 0, groups = 0;
+            const bool tc_v = module_tc_operands(visibility, &dv, &pk.vis.weights_op, &pk.vis.table, &kv);
+            const bool tc_t = module_tc_operands(throughput, &dt, &pk.thr.weights_op, &pk.thr.table, &kt);
+            int candidates[2] = {0, 0}, n_candidates = 0;
+            if (tc_v && tc_t && kv == kt) {
+                for (int g : {4, 6})
+                    if (render_pk_supported(*dv, *dt, g)) candidates[n_candidates++] = g;
+            }
+            if (n_candidates) groups = candidates[0];
+            if (p->mode == NLOD_RENDER_PERSISTENT && !groups)
+                throw Error(NLOD_ERR_UNSUPPORTED, "the persistent form needs two tensor-core modules of one operand type with "
+                                                  "64-wide networks of 6 and 10 inputs");
+            if (p->mode != NLOD_RENDER_WAVEFRONT && groups) {
+                r->mode = NLOD_RENDER_PERSISTENT;
+                auto alloc = [&](size_t bytes) {
+                    void* q = dev_alloc<uint8_t>(bytes);
+                    r->owned.push_back(q);
+                    cuda_check(cudaMemset(q, 0, bytes), "memset");
+                    return q;
+                };
+                RenderBufs& B = r->B;
+                B.ctl = static_cast<Control*>(alloc(sizeof(Control)));
+                B.image = static_cast<float*>(alloc(sizeof(float) * 3 * (size_t)n));
+                B.ray_stats = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * 2 * (size_t)n));
+                B.status = static_cast<uint32_t*>(alloc(sizeof(uint32_t)));
+                pk.C = C;
+                pk.vis.max_level = p->lod_max_level;
+                pk.thr.max_level = 1000.f;
+                pk.image = B.image;
+                pk.ray_stats = B.ray_stats;
+                pk.ctl = B.ctl;
+                pk.status = B.status;
+                cuda_check(cudaStreamCreateWithFlags(&r->cap_stream, cudaStreamNonBlocking), "stream");
+                cudaStream_t s = r->cap_stream;
+                // Autotune: one frame per supported pipeline count, outside any capture (which also
+                // sets the kernels' shared-memory attributes); the fastest is captured.
+                float best = 0.f;
+                cudaEvent_t e0, e1;
+                cuda_check(cudaEventCreate(&e0), "event");
+                cuda_check(cudaEventCreate(&e1), "event");
+                for (int i = 0; i < n_candidates; ++i) {
+                    cuda_check(launch_render_pk(*dv, *dt, pk, kv, candidates[i], s), "persistent frame");   // warm-up
+                    cuda_check(cudaEventRecord(e0, s), "event");
+                    cuda_check(launch_render_pk(*dv, *dt, pk, kv, candidates[i], s), "persistent frame");
+                    cuda_check(cudaEventRecord(e1, s), "event");
+                    cuda_check(cudaEventSynchronize(e1), "synchronize");
+                    float ms = 0.f;
+                    cuda_check(cudaEventElapsedTime(&ms, e0, e1), "event");
+                    if (i == 0 || ms < best) {
+                        best = ms;
+                        groups = candidates[i];
+                    }
+                }
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                r->pk_groups = groups;
+                cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
+                const cudaError_t e = launch_render_pk(*dv, *dt, pk, kv, groups, s);
+                cudaGraph_t g = nullptr;
+                const cudaError_t e2 = cudaStreamEndCapture(s, &g);
+                r->graph = g;
+                cuda_check(e, "persistent frame graph");
+                cuda_check(e2, "persistent frame graph");
+                cuda_check(cudaGraphInstantiate(&r->exec, r->graph, 0), "graph instantiate");
+                *out = r.release();
+                return;
+            }
             auto alloc = [&](size_t bytes) {
                 void* q = dev_alloc<uint8_t>(bytes);
                 r->owned.push_back(q);
@@ -519,9 +453,13 @@ int nlod_render_stats(nlod_renderer* r, void* stream, uint64_t* out4) {
         out4[3] = c.dropped;
         if (st) {
             cuda_check(cudaMemset(r->B.status, 0, sizeof st), "status");
-            throw Error(NLOD_ERR_TIMEOUT, (st & 4u) ? "the frame exceeded its round bound" : "a ray exceeded its traversal step budget");
+            throw Error(NLOD_ERR_TIMEOUT, (st & 8u)   ? "a tensor-core wait of the persistent frame timed out"
+                                          : (st & 4u) ? "the frame exceeded its round or time bound"
+                                                      : "a ray exceeded its traversal step budget");
         }
     });
 }
+
+int nlod_renderer_mode(const nlod_renderer* r) { return r ? r->mode : -1; }
 
 }  // extern "C"

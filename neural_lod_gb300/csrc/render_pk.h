@@ -1,0 +1,35 @@
+// Launcher of the persistent render kernel (render_pk.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "desc.h"
+#include "render_common.cuh"
+
+namespace nlod {
+
+// One network's inference operands for the persistent kernel.
+struct PkNet {
+    const void* weights_op;   // inference weights, operand type, row-major [out][in] per layer
+    const void* table;        // parameter vector whose grid part the encoding gathers: the FP16
+                              // copy (FP16 form) or the FP32 inference parameters (BF16 form)
+    float max_level;          // grid max-level fraction for every query of this network
+};
+
+struct PkArgs {
+    render::RenderConsts C;
+    PkNet vis, thr;
+    float* image;             // [n_rays][3]
+    uint32_t* ray_stats;      // [n_rays][2] visibility / throughput queries per ray
+    render::Control* ctl;     // cnt[0] is the ray queue; totals as in the wavefront form
+    uint32_t* status;         // 2: DDA step budget, 4: frame time bound, 8: MMA wait timed out
+};
+
+// Whether the persistent kernel can run these two networks with `groups` tile pipelines per CTA.
+bool render_pk_supported(const ModelDesc& dv, const ModelDesc& dt, int groups);
+// Resets the frame's control words and launches one persistent frame (kind 1 = FP16, 2 = BF16).
+cudaError_t launch_render_pk(const ModelDesc& dv, const ModelDesc& dt, const PkArgs& a, int kind, int groups, cudaStream_t s);
+
+}  // namespace nlod

@@ -97,6 +97,24 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
     // leaves before staging weights and allocating TMEM.  The test is uniform over the CTA.
     if (blockIdx.x * G >= forward_rows(a) / kTcTile) return;
 
+    // Grid tables into L2 ahead of the gathers, when the batch touches most of their entries
+    // (rows x levels x 8 corners >= entries): each CTA prefetches its slice in 4 KB pieces.  A
+    // batch that starts with a cold L2 then meets L2 latency instead of DRAM latency on its
+    // first gathers.  Tables start on 512-byte boundaries and span multiples of 32 bytes.
+    if (d.n_grids > 0 && d.n_params_encoding > 0) {
+        const uint32_t esz = std::is_same<T, __half>::value ? 2u : 4u;
+        const uint8_t* base = std::is_same<T, __half>::value ? static_cast<const uint8_t*>(a.grid_h) + 2u * d.n_params_network
+                                                             : reinterpret_cast<const uint8_t*>(a.params + d.n_params_network);
+        const uint64_t total = (uint64_t)d.n_params_encoding * esz;
+        const uint64_t touched = (uint64_t)forward_rows(a) * d.grids[0].n_levels * 8u * d.grids[0].n_features;
+        if (touched >= d.n_params_encoding) {
+            const uint64_t per = ((total + gridDim.x - 1) / gridDim.x + 15u) & ~uint64_t(15);
+            const uint64_t lo = (uint64_t)blockIdx.x * per, hi = lo + per < total ? lo + per : total;
+            for (uint64_t off = lo + (uint64_t)threadIdx.x * 4096u; off < hi; off += (uint64_t)blockDim.x * 4096u)
+                tc::prefetch_l2_bulk(base + off, (uint32_t)(hi - off < 4096u ? hi - off : 4096u));
+        }
+    }
+
     // ---- set-up: barriers, TMEM, resident weights ----
     if (tid == 0) {
         for (int g = 0; g < G; ++g) tc::mbar_init(&bars[g], 1);

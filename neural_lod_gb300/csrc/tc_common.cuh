@@ -69,6 +69,12 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
                  : "memory");
 }
 
+// Asynchronous prefetch of [src, src + bytes) from global memory into L2 (16-byte aligned source,
+// size a multiple of 16); fire-and-forget, nothing waits for it.
+__device__ __forceinline__ void prefetch_l2_bulk(const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // One arrival (release at CTA scope) on an mbarrier.
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");

@@ -1,12 +1,14 @@
-"""Wavefront neural-LoD render query (host-side mirror of the nlod_renderer C ABI).
+"""Neural-LoD render query (host-side mirror of the nlod_renderer C ABI).
 
     r = Renderer(visibility_module, throughput_module, lod_grid, RenderParams(width=1024, height=1024, level=3))
     image = r.frame()                      # cuda float32 [height, width, 3]
     vis_q, thr_q, rounds, dropped = r.stats()
 
-A frame is one CUDA-graph launch: every ray advances one query per round inside a conditional
-while node (no host round trip per wavefront, unlike the reference's voxel_tracing loop in
-rptr/cuda/neural-lod/wavefront_neural_throughput_visibility_lod.cu:470-720).
+A frame is one CUDA-graph launch with no host round trip per wavefront (unlike the reference's
+voxel_tracing loop in rptr/cuda/neural-lod/wavefront_neural_throughput_visibility_lod.cu:470-720),
+in one of two forms that give the same pixels: one persistent kernel whose tile pipelines refill
+their ray slots from a queue (tensor-core modules; the default), or rounds in a conditional
+while node in which every ray advances one query (MODE_WAVEFRONT, and the FP32 modules).
 """
 from __future__ import annotations
 
@@ -20,7 +22,9 @@ class _Params(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("level", C.c_uint32), ("max_depth", C.c_uint32),
                 ("max_vis_queries", C.c_uint32), ("threshold", C.c_float), ("eye", C.c_float * 3), ("target", C.c_float * 3),
                 ("up", C.c_float * 3), ("fov_y_deg", C.c_float), ("background", C.c_float * 3), ("env_color", C.c_float * 3),
-                ("lod_max_level", C.c_float), ("lod_input", C.c_float), ("seed", C.c_uint64)]
+                ("lod_max_level", C.c_float), ("lod_input", C.c_float), ("seed", C.c_uint64), ("mode", C.c_uint32)]
+
+MODE_AUTO, MODE_WAVEFRONT, MODE_PERSISTENT = 0, 1, 2     # NLOD_RENDER_*
 
 
 @dataclass
@@ -40,12 +44,13 @@ class RenderParams:
     lod_max_level: float = 1000.0
     lod_input: float = 0.0
     seed: int = 1337
+    mode: int = MODE_AUTO
     extra: dict = field(default_factory=dict)
 
     def to_c(self) -> _Params:
         p = _Params()
         for k in ("width", "height", "level", "max_depth", "max_vis_queries", "threshold", "fov_y_deg", "lod_max_level",
-                  "lod_input", "seed"):
+                  "lod_input", "seed", "mode"):
             setattr(p, k, getattr(self, k))
         for k in ("eye", "target", "up", "background", "env_color"):
             getattr(p, k)[:] = [float(v) for v in getattr(self, k)]
@@ -88,6 +93,11 @@ class Renderer:
         check(self._lib.nlod_render_frame(self._r, _stream(stream), image.data_ptr(),
                                           None if ray_stats is None else ray_stats.data_ptr()))
         return image
+
+    @property
+    def mode(self) -> int:
+        """MODE_PERSISTENT (one persistent kernel per frame) or MODE_WAVEFRONT (rounds)."""
+        return int(self._lib.nlod_renderer_mode(self._r))
 
     def stats(self, stream=None):
         """(visibility queries, throughput queries, rounds, dropped rays) of the last frame; syncs."""

@@ -2,7 +2,7 @@
 
     python profile_run.py query  [--precision fp16] [--n 2097152] [--iters 3]
     python profile_run.py train  [--precision fp16] [--n 262144]  [--iters 3]
-    python profile_run.py render [--precision fp16] [--iters 3]
+    python profile_run.py render [--precision fp16] [--iters 3] [--mode 0|1|2] [--size 1024]
     python profile_run.py voxelize [--iters 3]
     python profile_run.py sampler  [--iters 3]
 
@@ -26,6 +26,8 @@ def main():
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--iters", type=int, default=3)
     ap.add_argument("--variant", type=int, default=-1, help="tensor-core kernel variant (-1: autotune)")
+    ap.add_argument("--mode", type=int, default=0, help="render form: 0 auto, 1 wavefront, 2 persistent")
+    ap.add_argument("--size", type=int, default=1024, help="render image width and height")
     a = ap.parse_args()
 
     import numpy as np
@@ -73,11 +75,11 @@ def main():
         rt = N.NetworkWithInputEncoding(10, 3, henc, hnet, precision=a.precision)
         rv.set_params(W.xavier_params(N.layout(venc, vnet, 6, 1), seed=12))
         rt.set_params(W.xavier_params(N.layout(henc, hnet, 10, 3), seed=13))
-        p = RenderParams(width=1024, height=1024, level=3, lod_max_level=4 / 8, lod_input=3.5 / 8, seed=42)
+        p = RenderParams(width=a.size, height=a.size, level=3, lod_max_level=4 / 8, lod_input=3.5 / 8, seed=42, mode=a.mode)
         r = Renderer(rv, rt, pyr, p)
         for _ in range(a.iters):
             r.frame()
-        print("stats", r.stats())
+        print("stats", r.stats(), "form", r.mode)
         n = p.width * p.height
         m = rv
     elif a.what == "sampler":

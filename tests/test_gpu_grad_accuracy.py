@@ -3,15 +3,27 @@ training workload: batch 2^18, 16-level grid + SH 4 -> 64 -> 64 -> 1 sigmoid, BC
 (beta 0.9 / 0.99, eps 1e-15), binary transmittance targets by exact DDA through a seeded 256^3
 value-noise occupancy (30 % occupied).
 
-The module first takes 100 Adam steps from the seeded start, so that the gradient is not the
-heavily cancelling one of a random start.  At that point the gradients of one step (no optimizer)
+The module first takes Adam steps from the seeded start (10 and 30: trained well past the random
+start, where the per-sample gradients cancel heavily, but short of the saturated fit that 100
+steps reach on this batch, where most outputs sit at BCE's clamp and the loss is 1e-5).  At that point the gradients of one step (no optimizer)
 of the FP16 and BF16 tensor-core forms and of the plain FP32 form are compared, per parameter
 block, with the FP64 oracle's analytic gradient, which is itself checked against FP64 central
 differences (h = 1e-4) on sampled parameters.  Also reported: the relative error over 1,024
 sampled parameters with a nonzero gradient.
 
-Bounds (relative L2 error per block):  FP32 form 1e-4;  FP16 and BF16 forms as stated in
-FP16_BOUND / BF16_BOUND below, from the measurement printed by this test.
+Bounds (relative L2 error per block), from the measurements printed by this test on a GB300:
+  after 10 steps (BCE 0.42; the oracle gradient agrees with central differences to a median 7e-7)
+      FP32 form  every block 1e-4 (measured <= 2.1e-5)
+      FP16 form  the network weights 1e-3 (measured 5.5-8.6e-4), the grid tables 1e-2 (4.4e-3),
+                 1,024 sampled parameters 1e-3 (3.3e-4)
+      BF16 form  every block 3e-2 (measured <= 1.3e-2)
+  after 30 steps (BCE 0.14; many outputs reach the loss's clamp at 1e-5 / 1 - 1e-5, where the
+  loss is not differentiable, so central differences no longer pin the gradient and the FP16
+  forward's rounding is felt by the nearly fitted samples)
+      FP32 1e-4 (measured <= 1e-6), FP16 3e-2 (measured <= 1.4e-2), BF16 8e-2 (measured <= 4.1e-2).
+The grid-table gradients of the FP16 form are sums over the few samples that touch each entry,
+evaluated with FP16 tables, FP16 encoded features and FP16 activations (tiny-cuda-nn's own
+precision); the network weights' gradients sum over every sample and meet 1e-3.
 """
 import numpy as np
 import pytest
@@ -22,9 +34,9 @@ from neural_lod_gb300 import NetworkWithInputEncoding, workloads as W
 pytestmark = pytest.mark.gpu
 
 N = 1 << 18
-FP16_BOUND = 1e-2
-BF16_BOUND = 8e-2
-FP32_BOUND = 1e-4
+# (steps) -> precision -> (network-weight blocks, grid block, 1,024 sampled parameters)
+BOUNDS = {10: {"fp32": (1e-4, 1e-4, 1e-4), "fp16": (1e-3, 1e-2, 1e-3), "bf16": (3e-2, 3e-2, 3e-2)},
+          30: {"fp32": (1e-4, 1e-4, 1e-4), "fp16": (3e-2, 3e-2, 3e-2), "bf16": (8e-2, 8e-2, 8e-2)}}
 
 
 def _rel(a, b):
@@ -33,8 +45,8 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-@pytest.fixture(scope="module")
-def trained(cuda, nlod_lib):
+@pytest.fixture(scope="module", params=[10, 30])
+def trained(request, cuda, nlod_lib):
     import torch
 
     from neural_lod_gb300 import samples as S
@@ -51,19 +63,22 @@ def trained(cuda, nlod_lib):
     m = NetworkWithInputEncoding(6, 1, enc, net, loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER, precision="fp16")
     m.set_params(params0)
     first = m.training_step(xd, td).item()
-    for _ in range(99):
+    for _ in range(request.param - 1):
         last = m.training_step(xd, td)
     m.sync_status()
-    print(f"\nBCE loss: step 1 {first:.5f}, step 100 {last.item():.5f}")
+    print(f"\nBCE loss: step 1 {first:.5f}, step {request.param} {last.item():.5f}")
     p = m.get_params("params").astype(np.float32)
     orc = oracle.Oracle(enc, net, 6, 1)
     loss64, g64 = orc.loss_and_grad("BinaryCrossEntropy", x, p.astype(np.float64), t)
-    return dict(x=x, t=t, xd=xd, td=td, enc=enc, net=net, spec=spec, p=p, orc=orc, loss64=loss64, g64=g64)
+    return dict(steps=request.param, x=x, t=t, xd=xd, td=td, enc=enc, net=net, spec=spec, p=p, orc=orc, loss64=loss64, g64=g64)
 
 
 def test_oracle_gradient_is_central_differences_at_the_trained_point(trained):
     """The FP64 analytic gradient against FP64 central differences (h = 1e-4) of the full-batch
-    loss, on MLP weights and touched grid entries."""
+    loss, on MLP weights and touched grid entries (at the 10-step point: past it the clamp of the
+    loss makes the difference quotients meaningless for saturated samples)."""
+    if trained["steps"] != 10:
+        pytest.skip("central differences are checked at the 10-step point")
     orc, x, t, g = trained["orc"], trained["x"], trained["t"], trained["g64"]
     p = trained["p"].astype(np.float64)
     n_net = trained["spec"]["n_params_network"]
@@ -110,9 +125,9 @@ def test_gradient_accuracy_at_trained_point(trained, precision):
     idx = np.random.default_rng(11).choice(nz, 1024, replace=False)
     sampled = _rel(g[idx], g64[idx])
     loss_err = abs(loss - trained["loss64"]) / trained["loss64"]
-    print(f"\n{precision}: loss rel {loss_err:.2e}; 1,024 sampled params rel {sampled:.2e}; " +
+    print(f"\n{trained['steps']} steps, {precision}: loss rel {loss_err:.2e}; 1,024 sampled params rel {sampled:.2e}; " +
           "; ".join(f"{k} {v:.2e}" for k, v in blocks.items()))
-    bound = {"fp16": FP16_BOUND, "bf16": BF16_BOUND, "fp32": FP32_BOUND}[precision]
+    b_net, b_grid, b_sampled = BOUNDS[trained["steps"]][precision]
     for k, v in blocks.items():
-        assert v <= bound, (precision, k, v)
-    assert sampled <= bound
+        assert v <= (b_grid if k == "grid" else b_net), (precision, k, v)
+    assert sampled <= b_sampled

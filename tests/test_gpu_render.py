@@ -1,18 +1,22 @@
-"""GPU parity of the wavefront render query (nlod_renderer: one CUDA-graph launch per frame with a
-conditional while loop over rounds) against the host restatement oracle.render.
+"""GPU parity of the render query (nlod_renderer: one CUDA-graph launch per frame, either the
+persistent kernel or rounds in a conditional while loop) against the host restatement
+oracle.render, and of the two forms against each other.
 
 Rays, voxel traversal and direction sampling are bit-identical on both sides; the networks are
 FP32 / FP16 on the GPU and FP64 on the host, so a ray's path can differ only where a visibility
 value lies within the networks' rounding distance of the threshold.  Tolerances: FP32 form -
 per-ray query counts equal for >= 99.5% of the rays and their pixels within 1e-3 relative;
-FP16 form - counts equal for >= 97% of the rays and those pixels within 2e-2 relative."""
+FP16 form - counts equal for >= 97% of the rays and those pixels within 2e-2 relative.
+The persistent form and the wavefront form run the same per-ray steps and network arithmetic, so
+their pixels, per-ray query counts and totals are identical bits (FP16 and BF16 modules)."""
 import numpy as np
 import pytest
 
 import oracle
 from neural_lod_gb300 import NetworkWithInputEncoding, workloads as W
 from neural_lod_gb300.lod import LodGrid
-from neural_lod_gb300.render import RenderParams, Renderer, camera
+from neural_lod_gb300 import NlodError
+from neural_lod_gb300.render import MODE_PERSISTENT, MODE_WAVEFRONT, RenderParams, Renderer, camera
 
 pytestmark = pytest.mark.gpu
 
@@ -40,6 +44,7 @@ def _render_both(precision, params, bits, res, levels):
     vm, tm, vo, to, vp, tp = _nets(precision)
     grid = LodGrid(bits, res, levels)
     r = Renderer(vm, tm, grid, params)
+    assert r.mode == (MODE_WAVEFRONT if precision == "fp32" or params.mode == MODE_WAVEFRONT else MODE_PERSISTENT)
     n = params.width * params.height
     stats = torch.zeros((n, 2), dtype=torch.int32, device="cuda")
     img = r.frame(ray_stats=stats).cpu().numpy()
@@ -52,10 +57,12 @@ def _render_both(precision, params, bits, res, levels):
     return img, stats.cpu().numpy().astype(np.uint32), tot, ref_img, ref_stats, ref_tot
 
 
-@pytest.mark.parametrize("precision,frac,rel", [("fp32", 0.995, 1e-3), ("fp16", 0.97, 2e-2)])
-def test_render_matches_oracle(cuda, nlod_lib, precision, frac, rel):
+@pytest.mark.parametrize("precision,frac,rel,mode", [("fp32", 0.995, 1e-3, 0), ("fp16", 0.97, 2e-2, MODE_PERSISTENT),
+                                                      ("fp16", 0.97, 2e-2, MODE_WAVEFRONT)])
+def test_render_matches_oracle(cuda, nlod_lib, precision, frac, rel, mode):
     bits, res, levels = _scene()
-    params = RenderParams(width=96, height=64, level=1, max_depth=4, max_vis_queries=24, lod_max_level=6 / 8, lod_input=1.5 / 8)
+    params = RenderParams(width=96, height=64, level=1, max_depth=4, max_vis_queries=24, lod_max_level=6 / 8, lod_input=1.5 / 8,
+                          mode=mode)
     img, st, tot, ref_img, ref_st, ref_tot = _render_both(precision, params, bits, res, levels)
     same = np.all(st == ref_st, axis=1)
     print(precision, "rays with identical query counts", same.mean(), "totals", tot, ref_tot)
@@ -82,3 +89,46 @@ def test_render_empty_grid_and_query_cap(cuda, nlod_lib):
     assert np.array_equal(st, ref_st)
     assert tot[3] == ref_tot[2] > 0          # dropped rays
     assert np.array_equal(img, ref_img)
+
+
+def _frame(precision, params, grid, mode):
+    import torch
+
+    vm, tm, vo, to, vp, tp = _nets(precision)
+    p = RenderParams(**{**params.__dict__, "mode": mode})
+    r = Renderer(vm, tm, grid, p)
+    assert r.mode == mode
+    n = p.width * p.height
+    stats = torch.zeros((n, 2), dtype=torch.int32, device="cuda")
+    img = r.frame(ray_stats=stats).cpu().numpy()
+    tot = r.stats()
+    img2 = r.frame().cpu().numpy()
+    assert np.array_equal(img, img2)
+    r.close()
+    return img, stats.cpu().numpy(), tot
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+@pytest.mark.parametrize("shape", [(96, 64, 1, 24), (257, 131, 0, 9)])
+def test_persistent_form_matches_wavefront_form(cuda, nlod_lib, precision, shape):
+    """Same pixels, same per-ray query counts, same totals; ray counts that are not a multiple of a
+    tile and a query cap that drops rays included."""
+    w, h, level, cap = shape
+    bits, res, levels = _scene()
+    grid = LodGrid(bits, res, levels)
+    params = RenderParams(width=w, height=h, level=level, max_depth=4, max_vis_queries=cap, lod_max_level=6 / 8, lod_input=1.5 / 8)
+    img_p, st_p, tot_p = _frame(precision, params, grid, MODE_PERSISTENT)
+    img_w, st_w, tot_w = _frame(precision, params, grid, MODE_WAVEFRONT)
+    print(f"{precision} {w}x{h}: persistent totals {tot_p}, wavefront {tot_w}")
+    assert np.array_equal(st_p, st_w)
+    assert np.array_equal(img_p.view(np.uint32), img_w.view(np.uint32))
+    assert tot_p[0] == tot_w[0] and tot_p[1] == tot_w[1] and tot_p[3] == tot_w[3]
+    assert tot_p[1] > 0
+
+
+def test_persistent_form_needs_tensor_core_modules(cuda, nlod_lib):
+    bits, res, levels = _scene()
+    grid = LodGrid(bits, res, levels)
+    vm, tm, *_ = _nets("fp32")
+    with pytest.raises(NlodError):
+        Renderer(vm, tm, grid, RenderParams(width=32, height=32, level=1, mode=MODE_PERSISTENT))
