@@ -4,9 +4,13 @@ Headline workload: the throughput query forward at batch 2^21 (16-level hash gri
 entries/level + two degree-4 SH encodings + LoD one-hot -> 80-wide input -> 4 x 64 ReLU -> 3
 exp outputs), FP16 tcgen05 form, inputs resident in HBM.  A "step" is one fused query launch
 over the whole batch.  Also reported: the same workload in the plain FP32 form, the end-to-end
-call from pinned host buffers, the visibility query (batch 65,536) and the visibility training
-step (batch 2^18, fwd + BCE + bwd + Adam) in both forms, the FP64-oracle error and a scalar FP32
-CPU baseline of the same encoding + MLP.
+call from pinned host buffers, the visibility query (batch 65,536), the visibility and throughput
+training steps (fwd + loss + bwd + Adam), the render frame, the sample generator, the voxelizer,
+the voxelize + train run, the FP64-oracle error, a scalar FP32 CPU baseline of the same encoding
++ MLP, and tiny-cuda-nn built from the reference's sources on the same GPU and workloads (live
+when oracle/_ref holds its build, else the figures committed in profiles/tcnn_comparison.md).
+Times are the median of the timed steps (p99 and mean beside the headline), each step between
+CUDA events on the launching stream.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -216,14 +220,14 @@ def _tcnn_comparison(dev, flush, args, T):
     out = torch.empty((n, 3), device=dev)
     tm = T.TcnnModel(17, 3, enc, net)
     tm.set_params(params)
-    t_tc = statistics.mean(time_steps(lambda: tm.inference(x, out), steps, 3, flush))
+    t_tc = statistics.median(time_steps(lambda: tm.inference(x, out), steps, 3, flush))
     ref = oracle.Oracle(enc, net, 17, 3).forward(xh[:4096], params)
     err_tc = float(np.abs(tm.inference(x[:4096]).cpu().numpy() - ref).mean())
     del tm
     mo = NetworkWithInputEncoding(17, 3, enc, net, precision="fp16")
     mo.set_params(params)
     mo.autotune(x, out)
-    t_ours = statistics.mean(time_steps(lambda: mo.inference(x, out), steps, 3, flush))
+    t_ours = statistics.median(time_steps(lambda: mo.inference(x, out), steps, 3, flush))
     err_ours = float(np.abs(mo.inference(x[:4096]).cpu().numpy() - ref).mean())
     del mo
     res["throughput_query"] = {"batch": n, "tcnn_queries_per_s": n / (t_tc * 1e-3), "ours_queries_per_s": n / (t_ours * 1e-3),
@@ -240,12 +244,12 @@ def _tcnn_comparison(dev, flush, args, T):
     tm = T.TcnnModel(6, 1, venc, vnet)
     tm.set_params(vparams)
     tm.set_max_level_gpu(fd)
-    t_tc = statistics.mean(time_steps(lambda: tm.inference(xvd, ov), args.steps, 3, flush))
+    t_tc = statistics.median(time_steps(lambda: tm.inference(xvd, ov), args.steps, 3, flush))
     del tm
     mo = NetworkWithInputEncoding(6, 1, venc, vnet, precision="fp16")
     mo.set_params(vparams)
     mo.set_max_level_gpu(fd)
-    t_ours = statistics.mean(time_steps(lambda: mo.inference(xvd, ov), args.steps, 3, flush))
+    t_ours = statistics.median(time_steps(lambda: mo.inference(xvd, ov), args.steps, 3, flush))
     del mo
     res["visibility_query"] = {"batch": nv, "tcnn_queries_per_s": nv / (t_tc * 1e-3), "ours_queries_per_s": nv / (t_ours * 1e-3),
                                "ours_over_tcnn": t_tc / t_ours}
@@ -256,12 +260,12 @@ def _tcnn_comparison(dev, flush, args, T):
         xd_, td_ = torch.from_numpy(xt).to(dev), torch.from_numpy(tt).to(dev)
         tm_ = T.TcnnModel(n_in, n_out, enc_, net_, loss, opt)
         tm_.set_params(pr)
-        t1 = statistics.mean(time_steps(lambda: tm_.training_step(xd_, td_), steps, 3, flush))
+        t1 = statistics.median(time_steps(lambda: tm_.training_step(xd_, td_), steps, 3, flush))
         del tm_
         mo_ = NetworkWithInputEncoding(n_in, n_out, enc_, net_, loss=loss, optimizer=opt, precision="fp16")
         mo_.set_params(pr)
         lo = torch.empty(1, device=dev)
-        t2 = statistics.mean(time_steps(lambda: mo_.training_step(xd_, td_, lo), steps, 3, flush))
+        t2 = statistics.median(time_steps(lambda: mo_.training_step(xd_, td_, lo), steps, 3, flush))
         del mo_
         nb = xt.shape[0]
         return {"batch": nb, "tcnn_samples_per_s": nb / (t1 * 1e-3), "ours_samples_per_s": nb / (t2 * 1e-3),
@@ -334,8 +338,8 @@ def run_reference(args, world, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -401,9 +405,12 @@ def main():
     clocks = clk.summary()
     torch.cuda.synchronize()
     m16.sync_status()
-    ms16 = statistics.mean(times16)
+    ms16 = statistics.median(times16)
+    t_sorted = sorted(times16)
+    ms16_p99 = t_sorted[min(len(t_sorted) - 1, int(round(0.99 * (len(t_sorted) - 1))))]
+    ms16_mean = statistics.mean(times16)
     times32 = time_steps(lambda: m32.inference(x, out), max(3, args.steps // 4), 3, flush)
-    ms32 = statistics.mean(times32)
+    ms32 = statistics.median(times32)
 
     # ---- end to end through the public API from pinned host buffers ----
     # (nlod_inference_host: the kernel reads the pinned input in place over NVLink-C2C, the output
@@ -415,7 +422,7 @@ def main():
         m16.inference_host(x_pin, out_pin)
 
     times_e2e = time_steps(e2e_step, max(3, args.steps // 2), 3, flush, barrier=pg.barrier if pg else None)
-    ms_e2e = statistics.mean(times_e2e)
+    ms_e2e = statistics.median(times_e2e)
 
     # ---- visibility query, batch 65,536 ----
     nv = W.WORKLOADS["visibility_query"]["batch"]
@@ -431,7 +438,7 @@ def main():
         mv.set_max_level_gpu(fracd)
         ov = torch.empty((nv, 1), device=dev)
         tv = time_steps(lambda: mv.inference(xvd, ov), args.steps, 3, flush)
-        vis[prec] = nv / (statistics.mean(tv) * 1e-3)
+        vis[prec] = nv / (statistics.median(tv) * 1e-3)
         del mv
 
     # ---- training steps: visibility (2^18, BCE) and throughput (2^20, RelativeL2, EMA/decay Adam) ----
@@ -447,7 +454,7 @@ def main():
             steps = max(3, args.steps // 2) if prec != "fp32" else max(3, args.steps // 4)
             tr = time_steps(lambda: mt.training_step(xd_, td_, lo), steps, 3, flush)
             mt.sync_status()
-            res[prec] = statistics.mean(tr)
+            res[prec] = statistics.median(tr)
             del mt
         return res
 
@@ -478,7 +485,7 @@ def main():
         vbits.zero_()
         V.voxelize(mesh, 1024, vb, vu, out=vbits)
 
-    tvox = statistics.mean(time_steps(vox_step, max(3, args.steps // 2), 3, flush))
+    tvox = statistics.median(time_steps(vox_step, max(3, args.steps // 2), 3, flush))
     vox_step()
     del mesh
     torch.cuda.synchronize()
@@ -551,8 +558,8 @@ def main():
         p50 = ft_sorted[len(ft) // 2]
         p99 = ft_sorted[min(len(ft) - 1, int(round(0.99 * (len(ft) - 1))))]
         render[form] = {"p50_ms": p50, "p99_ms": p99, "frames": len(ft), "vis_queries": q[0], "thr_queries": q[1],
-                        "rounds": q[2], "dropped_rays": q[3], "queries_per_s": (q[0] + q[1]) / (statistics.mean(ft) * 1e-3),
-                        "form": "persistent kernel" if rr.mode == 2 else "wavefront rounds"}
+                        "rounds": q[2], "dropped_rays": q[3], "queries_per_s": (q[0] + q[1]) / (statistics.median(ft) * 1e-3),
+                        "form": (f"persistent kernel, organisation {rr.mode & 0xFF}" if rr.persistent else "wavefront rounds")}
         rr.close()
         del rv, rt
     # host restatement on a bounded sample of the same frame (FP64 networks, all host threads)
@@ -577,8 +584,8 @@ def main():
         yg, _ = gsp.trace_throughput(qg, xg, 5)
         return gsp.compact(xg, yg)
 
-    t_gv = statistics.mean(time_steps(gen_vis, max(3, args.steps // 2), 3, flush))
-    t_gt = statistics.mean(time_steps(gen_thr, max(3, args.steps // 2), 3, flush))
+    t_gv = statistics.median(time_steps(gen_vis, max(3, args.steps // 2), 3, flush))
+    t_gt = statistics.median(time_steps(gen_thr, max(3, args.steps // 2), 3, flush))
     _, yv_ = gen_vis()
     occluded = float(yv_.mean())
     _, _, nv_ = gen_thr()
@@ -621,7 +628,8 @@ def main():
     achieved_tflops = FLOP_PER_QUERY * n / (ms16 * 1e-3) / 1e12
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": t_step, "ms_per_step_p99": ms16_p99, "ms_per_step_mean": ms16_mean, "timing": "median of the timed steps",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp16", "data": "synthetic (seeded PCG64 inputs, Xavier/U[-1e-4,1e-4] weights)",
         "config": {"workload": "throughput_query", "global_batch": n * world, "per_gpu_batch": n,
                    "encoding": "hashgrid L16 F2 T2^19 base16 s1.5 + SH4 x2 + onehot8 (80 wide)",

@@ -321,6 +321,10 @@ typedef struct nlod_render_params {
 #define NLOD_RENDER_AUTO 0
 #define NLOD_RENDER_WAVEFRONT 1
 #define NLOD_RENDER_PERSISTENT 2
+/* The persistent form with one organisation forced instead of autotuned (tests and tuning):
+ * f = 4 or 6 tile pipelines per CTA that march their own rays, or f = 8 or 16 marcher warps
+ * feeding two tensor-core groups (warp-specialized). */
+#define NLOD_RENDER_PERSISTENT_FORM(f) (0x100 | (f))
 
 /* Index-space camera of a level with res voxels per axis: eye[3], right[3] (scaled by
  * tan(fov/2) * aspect), up[3] (scaled by tan(fov/2)), forward[3].  Host only. */
@@ -339,7 +343,8 @@ NLOD_API int nlod_render_frame(nlod_renderer* r, void* stream, float* image, uin
  * NLOD_ERR_TIMEOUT if a ray ran out of DDA steps, the frame hit its round or time bound, or a
  * tensor-core wait timed out. */
 NLOD_API int nlod_render_stats(nlod_renderer* r, void* stream, uint64_t* out4);
-/* The form the renderer runs: NLOD_RENDER_WAVEFRONT or NLOD_RENDER_PERSISTENT. */
+/* The form the renderer runs: NLOD_RENDER_WAVEFRONT, or NLOD_RENDER_PERSISTENT_FORM(f) with the
+ * persistent organisation the autotune (or the caller) chose. */
 NLOD_API int nlod_renderer_mode(const nlod_renderer* r);
 
 /* ---- Per-voxel visibility thresholds ----------------------------------------------------------

@@ -285,17 +285,27 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             int kv = 0, kt = 0, groups = 0;
             const bool tc_v = module_tc_operands(visibility, &dv, &pk.vis.weights_op, &pk.vis.table, &kv);
             const bool tc_t = module_tc_operands(throughput, &dt, &pk.thr.weights_op, &pk.thr.table, &kt);
-            int candidates[2] = {0, 0}, n_candidates = 0;
+            int candidates[4] = {0, 0, 0, 0}, n_candidates = 0;
             if (tc_v && tc_t && kv == kt) {
-                for (int g : {4, 6})
+                for (int g : {kWsForm16, kWsForm8, 4, 6})
                     if (render_pk_supported(*dv, *dt, g)) candidates[n_candidates++] = g;
             }
+            if ((p->mode & 0x100u) != 0) {
+                // one organisation forced
+                const int f = (int)(p->mode & 0xFFu);
+                bool ok = false;
+                for (int i = 0; i < n_candidates; ++i) ok |= candidates[i] == f;
+                if (!ok) throw Error(NLOD_ERR_UNSUPPORTED, "persistent organisation " + std::to_string(f) + " is not available for these modules");
+                candidates[0] = f;
+                n_candidates = 1;
+            } else if (p->mode != NLOD_RENDER_AUTO && p->mode != NLOD_RENDER_WAVEFRONT && p->mode != NLOD_RENDER_PERSISTENT) {
+                throw Error(NLOD_ERR_INVALID, "unknown render mode");
+            }
             if (n_candidates) groups = candidates[0];
-            if (p->mode == NLOD_RENDER_PERSISTENT && !groups)
+            if (p->mode != NLOD_RENDER_AUTO && p->mode != NLOD_RENDER_WAVEFRONT && !groups)
                 throw Error(NLOD_ERR_UNSUPPORTED, "the persistent form needs two tensor-core modules of one operand type with "
                                                   "64-wide networks of 6 and 10 inputs");
             if (p->mode != NLOD_RENDER_WAVEFRONT && groups) {
-                r->mode = NLOD_RENDER_PERSISTENT;
                 auto alloc = [&](size_t bytes) {
                     void* q = dev_alloc<uint8_t>(bytes);
                     r->owned.push_back(q);
@@ -338,6 +348,7 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
                 cudaEventDestroy(e0);
                 cudaEventDestroy(e1);
                 r->pk_groups = groups;
+                r->mode = NLOD_RENDER_PERSISTENT_FORM(groups);
                 cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
                 const cudaError_t e = launch_render_pk(*dv, *dt, pk, kv, groups, s);
                 cudaGraph_t g = nullptr;

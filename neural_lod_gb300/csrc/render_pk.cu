@@ -366,6 +366,352 @@ __global__ void __launch_bounds__(G * kGroupThreads, 1)
     }
 }
 
+// ---- warp-specialized form --------------------------------------------------------------------
+// The tile pipelines above march their own rays between network passes, so the DDA's dependent
+// loads run with only G x 4 warps per SM to hide them, and each pipeline's barriers wait for its
+// slowest ray.  Here the two jobs are split: MW "marcher" warps own a pool of ray slots in shared
+// memory (K per lane) and do all ray generation and DDA marching; two four-warp tensor-core groups
+// own half of the slots each and run the networks on the slots whose queries are ready.  A slot's
+// state word says who holds it: EMPTY / MARCH belong to its marcher lane, VIS / THR to its network
+// group; a side hands a slot over by writing the ray data, a block fence, then the state (and
+// reads the state, a fence, then the data).  A group runs a full tile of 128 ready visibility
+// queries, or after a short wait whatever is ready, and a throughput pass whenever throughput
+// queries are ready.  The frame ends when the ray queue is exhausted and every slot is empty.
+
+enum : uint32_t { WS_EMPTY = 0, WS_MARCH = 1, WS_VIS = 2, WS_THR = 3 };
+
+template <int MW, int K>
+struct WsLayout {
+    static constexpr int kSlots = MW * 32 * K;
+    PkLayout base;            // weights, level tables, the two groups' A tiles (base.groups)
+    uint32_t rays, ray_id, counts, state, rows, ctl;
+    uint32_t total;
+};
+
+template <int MW, int K>
+__host__ __device__ inline WsLayout<MW, K> ws_layout(const ModelDesc& dv, const ModelDesc& dt) {
+    WsLayout<MW, K> L{};
+    L.base = pk_layout(dv, dt, 2);
+    uint32_t off = L.base.total;
+    constexpr uint32_t S = (uint32_t)WsLayout<MW, K>::kSlots;
+    L.rays = off;
+    off += S * (uint32_t)sizeof(RayState);
+    L.ray_id = off;
+    off += S * 4u;
+    L.counts = off;
+    off += S * 4u;
+    L.state = off;
+    off += S * 4u;
+    L.rows = off;             // per group: [2][128] slot of each visibility / throughput row, 2 counters
+    off += 2u * (2u * 128u + 4u) * 4u;
+    L.ctl = off;              // active marcher warps
+    off += 16u;
+    L.total = up128(off);
+    return L;
+}
+
+__device__ __forceinline__ uint32_t ld_state(const uint32_t* p) { return *reinterpret_cast<const volatile uint32_t*>(p); }
+__device__ __forceinline__ void st_state(uint32_t* p, uint32_t v) { *reinterpret_cast<volatile uint32_t*>(p) = v; }
+
+template <typename T, int MW, int K>
+__global__ void __launch_bounds__(2 * kGroupThreads + MW * 32, 1)
+    k_render_ws(const __grid_constant__ ModelDesc dv, const __grid_constant__ ModelDesc dt, const __grid_constant__ PkArgs A) {
+    using TT = typename std::conditional<std::is_same<T, __half>::value, __half, float>::type;
+    constexpr int kThreads = 2 * kGroupThreads + MW * 32;
+    constexpr uint32_t S = (uint32_t)WsLayout<MW, K>::kSlots;
+    constexpr uint32_t kHalf = S / 2u;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const WsLayout<MW, K> L = ws_layout<MW, K>(dv, dt);
+    const RenderConsts& C = A.C;
+    RayState* rays = reinterpret_cast<RayState*>(smem + L.rays);
+    uint32_t* ray_id = reinterpret_cast<uint32_t*>(smem + L.ray_id);
+    uint32_t* counts = reinterpret_cast<uint32_t*>(smem + L.counts);     // vis | thr << 16 of the slot's ray
+    uint32_t* state = reinterpret_cast<uint32_t*>(smem + L.state);
+    uint32_t* active_marchers = reinterpret_cast<uint32_t*>(smem + L.ctl);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.base.bar);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.base.bar + 16);
+
+    const uint32_t tid = threadIdx.x;
+    const uint32_t warp = tid >> 5, lane = tid & 31;
+    const unsigned long long t_start = globaltimer_ns();
+
+    // ---- set-up ----
+    if (tid == 0) {
+        tc::mbar_init(&bars[0], 1);
+        tc::mbar_init(&bars[1], 1);
+        tc::fence_barrier_init();
+        *active_marchers = MW;
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tmem_slot, L.base.tmem_cols);
+        tc::tmem_relinquish();
+    }
+    for (uint32_t i = tid; i < S; i += kThreads) st_state(&state[i], WS_EMPTY);
+    GridLevel* lvl_v = reinterpret_cast<GridLevel*>(smem + L.base.lv);
+    GridLevel* lvl_t = reinterpret_cast<GridLevel*>(smem + L.base.lt);
+    stage_network(dv, A.vis.weights_op, smem + L.base.wv, lvl_v, tid, kThreads);
+    stage_network(dt, A.thr.weights_op, smem + L.base.wt, lvl_t, tid, kThreads);
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+
+    if (warp >= 8) {
+        // ================= marcher warps =================
+        const uint32_t mlane = (warp - 8) * 32 + lane;      // 0 .. MW*32-1
+        bool queue_done = false;
+        for (uint32_t it = 0;; ++it) {
+            bool progress = false;
+            // march every slot handed back for marching
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const uint32_t s = mlane + (uint32_t)k * (MW * 32);
+                if (ld_state(&state[s]) == WS_MARCH) {
+                    __threadfence_block();
+                    RayState st = rays[s];
+                    const uint32_t ray = ray_id[s];
+                    const int mr = ray_march(C, st, A.image + 3 * (size_t)ray);
+                    if (mr == MARCH_VIS) {
+                        rays[s] = st;
+                        counts[s] += 1u;
+                        __threadfence_block();
+                        st_state(&state[s], WS_VIS);
+                    } else {
+                        if (mr == MARCH_DROPPED) atomicAdd(&A.ctl->dropped, 1u);
+                        else if (mr == MARCH_FAIL) atomicOr(A.status, 2u);
+                        const uint32_t c = counts[s];
+                        A.ray_stats[2 * ray] = c & 0xFFFFu;
+                        A.ray_stats[2 * ray + 1] = c >> 16;
+                        st_state(&state[s], WS_EMPTY);
+                    }
+                    progress = true;
+                }
+            }
+            // refill one empty slot per lane from the ray queue (warp-aggregated)
+            int empty_k = -1;
+#pragma unroll
+            for (int k = K - 1; k >= 0; --k)
+                if (ld_state(&state[mlane + (uint32_t)k * (MW * 32)]) == WS_EMPTY) empty_k = k;
+            const bool want = !queue_done && empty_k >= 0;
+            const unsigned m = __ballot_sync(kFull, want);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                uint32_t base = 0;
+                if ((int)lane == leader) base = atomicAdd(&A.ctl->cnt[0], (uint32_t)__popc(m));
+                base = __shfl_sync(kFull, base, leader);
+                if (want) {
+                    const uint32_t id = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+                    if (id >= C.n_rays) {
+                        queue_done = true;
+                    } else {
+                        const uint32_t s = mlane + (uint32_t)empty_k * (MW * 32);
+                        RayState st;
+                        ray_generate(C, id, st);
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) A.image[3 * (size_t)id + c] = 0.f;
+                        const int mr = ray_march(C, st, A.image + 3 * (size_t)id);
+                        if (mr == MARCH_VIS) {
+                            rays[s] = st;
+                            ray_id[s] = id;
+                            counts[s] = 1u;
+                            __threadfence_block();
+                            st_state(&state[s], WS_VIS);
+                        } else {
+                            if (mr == MARCH_DROPPED) atomicAdd(&A.ctl->dropped, 1u);
+                            else if (mr == MARCH_FAIL) atomicOr(A.status, 2u);
+                            A.ray_stats[2 * id] = 0u;
+                            A.ray_stats[2 * id + 1] = 0u;
+                        }
+                    }
+                }
+                progress = true;
+            }
+            // the lane is done when the queue is exhausted and all its slots are empty
+            bool mine_empty = true;
+#pragma unroll
+            for (int k = 0; k < K; ++k) mine_empty &= ld_state(&state[mlane + (uint32_t)k * (MW * 32)]) == WS_EMPTY;
+            if (__all_sync(kFull, queue_done && mine_empty)) break;
+            if (!__any_sync(kFull, progress)) {
+                if ((it & 63u) == 0 && globaltimer_ns() - t_start > kFrameNs) {
+                    if (lane == 0) atomicOr(A.status, 4u);
+                    break;
+                }
+                __nanosleep(256);
+            }
+        }
+        __threadfence_block();
+        if (lane == 0) atomicSub(active_marchers, 1u);
+    } else {
+        // ================= tensor-core groups =================
+        const uint32_t grp = warp >> 2;                     // 0 or 1
+        const uint32_t gtid = tid & (kGroupThreads - 1);
+        const uint32_t quarter = warp & 3u;
+        const uint32_t bar_id = 1u + grp;
+        const uint32_t row = gtid;
+        const uint32_t tmem_base = *tmem_slot + grp * (uint32_t)kWidth;
+        const uint32_t taddr_row = tmem_base + ((quarter * 32u) << 16);
+        uint8_t* a_tile = smem + L.base.groups + grp * L.base.group_stride;
+        float* in_row = reinterpret_cast<float*>(a_tile + L.base.in_rel) + row * kInLd;
+        const uint32_t a_addr = tc::smem_addr(a_tile);
+        uint64_t* bar = &bars[grp];
+        uint32_t* vis_rows = reinterpret_cast<uint32_t*>(smem + L.rows) + grp * (2u * 128u + 4u);
+        uint32_t* thr_rows = vis_rows + 128;
+        uint32_t* cnt = vis_rows + 256;                     // [0] visibility, [1] throughput ready
+        const TT* vtab = static_cast<const TT*>(A.vis.table);
+        const TT* ttab = static_cast<const TT*>(A.thr.table);
+        const uint32_t first = grp * kHalf;
+        uint32_t phase = 0;
+        bool aborted = false;
+        unsigned long long tot_v = 0, tot_t = 0;
+        uint32_t waited = 0, passes = 0;
+        for (uint32_t it = 0;; ++it) {
+            // ---- collect the ready slots of this group's half ----
+            if (gtid == 0) {
+                cnt[0] = 0u;
+                cnt[1] = 0u;
+            }
+            const bool marchers_gone = ld_state(active_marchers) == 0u;
+            group_sync(bar_id);
+            for (uint32_t j = gtid; j < kHalf; j += kGroupThreads) {
+                const uint32_t s = first + j;
+                const uint32_t v = ld_state(&state[s]);
+                if (v == WS_VIS) {
+                    const uint32_t pos = atomicAdd(&cnt[0], 1u);
+                    if (pos < 128u) vis_rows[pos] = s;
+                } else if (v == WS_THR) {
+                    const uint32_t pos = atomicAdd(&cnt[1], 1u);
+                    if (pos < 128u) thr_rows[pos] = s;
+                }
+            }
+            group_sync(bar_id);
+            const uint32_t n_vis = min(cnt[0], 128u), n_thr = min(cnt[1], 128u);
+            const bool timed_out = (it & 63u) == 0 && globaltimer_ns() - t_start > kFrameNs;
+            if (group_sync_or(bar_id, timed_out)) {
+                if (gtid == 0) atomicOr(A.status, 4u);
+                break;
+            }
+            // a full visibility tile, or after a short wait (or at the end) whatever is ready
+            const bool run_vis = n_vis == 128u || (n_vis > 0u && (waited >= 4u || marchers_gone));
+            const bool run_thr = n_thr > 0u && (n_thr == 128u || !run_vis);
+            if (!run_vis && !run_thr) {
+                if (marchers_gone && n_vis == 0u && n_thr == 0u) break;
+                ++waited;
+                __nanosleep(128);
+                continue;
+            }
+            waited = 0;
+            ++passes;
+            float out[3];
+            if (run_vis) {
+                __threadfence_block();
+                const bool mine = row < n_vis;
+                const uint32_t s = mine ? vis_rows[row] : 0u;
+                RayState st;
+                if (mine) {
+                    st = rays[s];
+                    vis_row(st, in_row);
+                    RowStore<T> rs{TcStore<T>{a_tile, dv.enc_width * 16u}, row};
+                    encode_tile_rows<kNL>(dv, lvl_v, vtab, in_row, kInLd, nullptr, A.vis.max_level, 0, 1, 0, 1, rs);
+                    ++tot_v;
+                }
+                tc::fence_proxy_async_smem();
+                tc::fence_before_sync();
+                group_sync(bar_id);
+                if (!run_mlp<T>(dv, smem + L.base.wv, a_tile, a_addr, tmem_base, taddr_row, bar, phase, bar_id, gtid, row, out)) {
+                    aborted = true;
+                    break;
+                }
+                if (mine) {
+                    const uint32_t ray = ray_id[s];
+                    const int vr = vis_resolve(C, st, ray, out[0]);
+                    rays[s] = st;
+                    if (vr == VIS_ACCEPT_THR) {
+                        counts[s] += 1u << 16;
+                        __threadfence_block();
+                        st_state(&state[s], WS_THR);
+                    } else if (vr == VIS_ACCEPT_END) {
+                        const uint32_t c = counts[s];
+                        A.ray_stats[2 * ray] = c & 0xFFFFu;
+                        A.ray_stats[2 * ray + 1] = c >> 16;
+                        __threadfence_block();
+                        st_state(&state[s], WS_EMPTY);
+                    } else {
+                        __threadfence_block();
+                        st_state(&state[s], WS_MARCH);
+                    }
+                }
+            }
+            if (run_thr) {
+                __threadfence_block();
+                const bool mine = row < n_thr;
+                const uint32_t s = mine ? thr_rows[row] : 0u;
+                RayState st;
+                if (mine) {
+                    st = rays[s];
+                    thr_row(C, st, in_row);
+                    RowStore<T> rs{TcStore<T>{a_tile, dt.enc_width * 16u}, row};
+                    encode_tile_rows<kNL>(dt, lvl_t, ttab, in_row, kInLd, nullptr, A.thr.max_level, 0, 1, 0, 1, rs);
+                    ++tot_t;
+                }
+                tc::fence_proxy_async_smem();
+                tc::fence_before_sync();
+                group_sync(bar_id);
+                if (!run_mlp<T>(dt, smem + L.base.wt, a_tile, a_addr, tmem_base, taddr_row, bar, phase, bar_id, gtid, row, out)) {
+                    aborted = true;
+                    break;
+                }
+                if (mine) {
+                    const float t3[3] = {out[0], out[1], out[2]};
+                    const bool alive = thr_resolve(st, t3);
+                    rays[s] = st;
+                    if (alive) {
+                        __threadfence_block();
+                        st_state(&state[s], WS_MARCH);
+                    } else {
+                        const uint32_t ray = ray_id[s], c = counts[s];
+                        A.ray_stats[2 * ray] = c & 0xFFFFu;
+                        A.ray_stats[2 * ray + 1] = c >> 16;
+                        __threadfence_block();
+                        st_state(&state[s], WS_EMPTY);
+                    }
+                }
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            tot_v += __shfl_xor_sync(kFull, tot_v, o);
+            tot_t += __shfl_xor_sync(kFull, tot_t, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&A.ctl->tot_vis, tot_v);
+            atomicAdd(&A.ctl->tot_thr, tot_t);
+            if (gtid == 0) atomicMax(&A.ctl->tot_rounds, (unsigned long long)passes);
+        }
+        if (aborted) {
+            (void)tc::mbar_wait_bounded(bar, phase ^ 1u, kWaitCycles);
+            if (gtid == 0) atomicOr(A.status, 8u);
+        }
+    }
+
+    // ---- teardown ----
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(*tmem_slot, L.base.tmem_cols);
+    }
+}
+
+template <typename T, int MW, int K>
+cudaError_t launch_ws(const ModelDesc& dv, const ModelDesc& dt, const PkArgs& a, int n_sms, cudaStream_t s) {
+    const WsLayout<MW, K> L = ws_layout<MW, K>(dv, dt);
+    if (L.total > 227u * 1024u) return cudaErrorInvalidConfiguration;
+    const uint32_t bytes = L.total > 120u * 1024u ? L.total : 120u * 1024u;
+    cudaError_t e = ensure_dynamic_smem((const void*)k_render_ws<T, MW, K>, bytes);
+    if (e != cudaSuccess) return e;
+    k_render_ws<T, MW, K><<<(uint32_t)n_sms, 2 * kGroupThreads + MW * 32, bytes, s>>>(dv, dt, a);
+    return cudaGetLastError();
+}
+
 __global__ void k_reset_pk(Control* ctl) {
     Control c{};
     *ctl = c;
@@ -397,6 +743,8 @@ bool render_pk_supported(const ModelDesc& dv, const ModelDesc& dt, int groups) {
         if (d->n_input + 1 > kInLd) return false;
     }
     if (dv.n_input != 6 || dt.n_input != 10) return false;
+    if (groups == kWsForm16) return ws_layout<16, 2>(dv, dt).total <= 227u * 1024u;
+    if (groups == kWsForm8) return ws_layout<8, 4>(dv, dt).total <= 227u * 1024u;
     if (groups != 4 && groups != 6) return false;
     return pk_layout(dv, dt, groups).total <= 227u * 1024u;
 }
@@ -408,6 +756,10 @@ cudaError_t launch_render_pk(const ModelDesc& dv, const ModelDesc& dt, const PkA
     if (e != cudaSuccess) return e;
     k_reset_pk<<<1, 1, 0, s>>>(a.ctl);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (kind == 1 && groups == kWsForm16) return launch_ws<__half, 16, 2>(dv, dt, a, n_sms, s);
+    if (kind == 1 && groups == kWsForm8) return launch_ws<__half, 8, 4>(dv, dt, a, n_sms, s);
+    if (kind == 2 && groups == kWsForm16) return launch_ws<__nv_bfloat16, 16, 2>(dv, dt, a, n_sms, s);
+    if (kind == 2 && groups == kWsForm8) return launch_ws<__nv_bfloat16, 8, 4>(dv, dt, a, n_sms, s);
     if (kind == 1 && groups == 6) return launch_pk<__half, 6>(dv, dt, a, n_sms, s);
     if (kind == 1 && groups == 4) return launch_pk<__half, 4>(dv, dt, a, n_sms, s);
     if (kind == 2 && groups == 6) return launch_pk<__nv_bfloat16, 6>(dv, dt, a, n_sms, s);

@@ -27,7 +27,13 @@ struct PkArgs {
     uint32_t* status;         // 2: DDA step budget, 4: frame time bound, 8: MMA wait timed out
 };
 
-// Whether the persistent kernel can run these two networks with `groups` tile pipelines per CTA.
+// Organisations of the persistent kernel: 4 or 6 = that many tile pipelines per CTA, each marching
+// its own rays; kWsForm16 / kWsForm8 = the warp-specialized form with 16 marcher warps (2 ray slots
+// per lane) or 8 (4 per lane) feeding two tensor-core groups.
+constexpr int kWsForm16 = 16;
+constexpr int kWsForm8 = 8;
+
+// Whether the persistent kernel can run these two networks in the given organisation.
 bool render_pk_supported(const ModelDesc& dv, const ModelDesc& dt, int groups);
 // Resets the frame's control words and launches one persistent frame (kind 1 = FP16, 2 = BF16).
 cudaError_t launch_render_pk(const ModelDesc& dv, const ModelDesc& dt, const PkArgs& a, int kind, int groups, cudaStream_t s);

@@ -27,6 +27,11 @@ class _Params(C.Structure):
 MODE_AUTO, MODE_WAVEFRONT, MODE_PERSISTENT = 0, 1, 2     # NLOD_RENDER_*
 
 
+def persistent_form(f: int) -> int:
+    """NLOD_RENDER_PERSISTENT_FORM(f): f = 4 / 6 tile pipelines, 8 / 16 marcher warps."""
+    return 0x100 | f
+
+
 @dataclass
 class RenderParams:
     width: int = 1024
@@ -96,8 +101,12 @@ class Renderer:
 
     @property
     def mode(self) -> int:
-        """MODE_PERSISTENT (one persistent kernel per frame) or MODE_WAVEFRONT (rounds)."""
+        """MODE_WAVEFRONT (rounds) or persistent_form(f) (one persistent kernel per frame)."""
         return int(self._lib.nlod_renderer_mode(self._r))
+
+    @property
+    def persistent(self) -> bool:
+        return (self.mode & 0x100) != 0
 
     def stats(self, stream=None):
         """(visibility queries, throughput queries, rounds, dropped rays) of the last frame; syncs."""

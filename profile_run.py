@@ -26,7 +26,7 @@ def main():
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--iters", type=int, default=3)
     ap.add_argument("--variant", type=int, default=-1, help="tensor-core kernel variant (-1: autotune)")
-    ap.add_argument("--mode", type=int, default=0, help="render form: 0 auto, 1 wavefront, 2 persistent")
+    ap.add_argument("--mode", type=int, default=0, help="render form: 0 auto, 1 wavefront, 2 persistent, 256+f one persistent organisation")
     ap.add_argument("--size", type=int, default=1024, help="render image width and height")
     a = ap.parse_args()
 
@@ -77,9 +77,13 @@ def main():
         rt.set_params(W.xavier_params(N.layout(henc, hnet, 10, 3), seed=13))
         p = RenderParams(width=a.size, height=a.size, level=3, lod_max_level=4 / 8, lod_input=3.5 / 8, seed=42, mode=a.mode)
         r = Renderer(rv, rt, pyr, p)
-        for _ in range(a.iters):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * a.iters)]
+        for i in range(a.iters):
+            ev[2 * i].record()
             r.frame()
-        print("stats", r.stats(), "form", r.mode)
+            ev[2 * i + 1].record()
+        torch.cuda.synchronize()
+        print("stats", r.stats(), "form", r.mode, "frame ms", [round(ev[2 * i].elapsed_time(ev[2 * i + 1]), 3) for i in range(a.iters)])
         n = p.width * p.height
         m = rv
     elif a.what == "sampler":

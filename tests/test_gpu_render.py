@@ -16,7 +16,7 @@ import oracle
 from neural_lod_gb300 import NetworkWithInputEncoding, workloads as W
 from neural_lod_gb300.lod import LodGrid
 from neural_lod_gb300 import NlodError
-from neural_lod_gb300.render import MODE_PERSISTENT, MODE_WAVEFRONT, RenderParams, Renderer, camera
+from neural_lod_gb300.render import MODE_PERSISTENT, MODE_WAVEFRONT, RenderParams, Renderer, camera, persistent_form
 
 pytestmark = pytest.mark.gpu
 
@@ -44,7 +44,7 @@ def _render_both(precision, params, bits, res, levels):
     vm, tm, vo, to, vp, tp = _nets(precision)
     grid = LodGrid(bits, res, levels)
     r = Renderer(vm, tm, grid, params)
-    assert r.mode == (MODE_WAVEFRONT if precision == "fp32" or params.mode == MODE_WAVEFRONT else MODE_PERSISTENT)
+    assert r.persistent == (precision != "fp32" and params.mode != MODE_WAVEFRONT)
     n = params.width * params.height
     stats = torch.zeros((n, 2), dtype=torch.int32, device="cuda")
     img = r.frame(ray_stats=stats).cpu().numpy()
@@ -108,16 +108,19 @@ def _frame(precision, params, grid, mode):
     return img, stats.cpu().numpy(), tot
 
 
+@pytest.mark.parametrize("form", [4, 6, 8, 16])
 @pytest.mark.parametrize("precision", ["fp16", "bf16"])
 @pytest.mark.parametrize("shape", [(96, 64, 1, 24), (257, 131, 0, 9)])
-def test_persistent_form_matches_wavefront_form(cuda, nlod_lib, precision, shape):
-    """Same pixels, same per-ray query counts, same totals; ray counts that are not a multiple of a
-    tile and a query cap that drops rays included."""
+def test_persistent_form_matches_wavefront_form(cuda, nlod_lib, precision, shape, form):
+    """Every persistent organisation (tile pipelines marching their own rays; marcher warps feeding
+    two tensor-core groups) against the wavefront rounds: same pixels, same per-ray query counts,
+    same totals; ray counts that are not a multiple of a tile and a query cap that drops rays
+    included."""
     w, h, level, cap = shape
     bits, res, levels = _scene()
     grid = LodGrid(bits, res, levels)
     params = RenderParams(width=w, height=h, level=level, max_depth=4, max_vis_queries=cap, lod_max_level=6 / 8, lod_input=1.5 / 8)
-    img_p, st_p, tot_p = _frame(precision, params, grid, MODE_PERSISTENT)
+    img_p, st_p, tot_p = _frame(precision, params, grid, persistent_form(form))
     img_w, st_w, tot_w = _frame(precision, params, grid, MODE_WAVEFRONT)
     print(f"{precision} {w}x{h}: persistent totals {tot_p}, wavefront {tot_w}")
     assert np.array_equal(st_p, st_w)
