@@ -249,6 +249,7 @@ def _tcnn_comparison(dev, flush, args, T):
     mo = NetworkWithInputEncoding(6, 1, venc, vnet, precision="fp16")
     mo.set_params(vparams)
     mo.set_max_level_gpu(fd)
+    mo.autotune(xvd, ov)
     t_ours = statistics.median(time_steps(lambda: mo.inference(xvd, ov), args.steps, 3, flush))
     del mo
     res["visibility_query"] = {"batch": nv, "tcnn_queries_per_s": nv / (t_tc * 1e-3), "ours_queries_per_s": nv / (t_ours * 1e-3),
@@ -437,6 +438,8 @@ def main():
         mv.set_params(vparams)
         mv.set_max_level_gpu(fracd)
         ov = torch.empty((nv, 1), device=dev)
+        if prec != "fp32":
+            mv.autotune(xvd, ov)     # the kernel organisation for this batch size
         tv = time_steps(lambda: mv.inference(xvd, ov), args.steps, 3, flush)
         vis[prec] = nv / (statistics.median(tv) * 1e-3)
         del mv
@@ -626,6 +629,20 @@ def main():
 
     pk = peaks()
     achieved_tflops = FLOP_PER_QUERY * n / (ms16 * 1e-3) / 1e12
+
+    def roof(bound, work, ms, note):
+        """Roofline entry of a leg: algorithmic FLOPs (tensor) or bytes (hbm) per step over its time."""
+        if bound == "tensor":
+            a = work / (ms * 1e-3) / 1e12
+            return {"bound": "tensor", "achieved": a, "peak": pk["bf16_tflops"], "unit": "TFLOP/s", "frac": a / pk["bf16_tflops"],
+                    "work_per_step": work, "note": note}
+        a = work / (ms * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": a, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": a / pk["hbm_gbs"], "work_per_step": work,
+                "note": note}
+
+    vis_train_params = 1_841_280           # 16-level visibility grid (1,833,088) + MLP (8,192)
+    thr_train_params = 13_045_424          # 16-level throughput grid (13,026,992) + MLP (18,432)
+    render_flop = {k: 12416 * v["vis_queries"] + FLOP_PER_QUERY * v["thr_queries"] for k, v in render.items()}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_step, "ms_per_step_p99": ms16_p99, "ms_per_step_mean": ms16_mean, "timing": "median of the timed steps",
@@ -648,21 +665,32 @@ def main():
         "visibility_train": {"batch": nt, "unit": "samples/s", "flop_per_sample": TRAIN_FLOP_PER_SAMPLE,
                              **{f"{p}_samples_per_s": nt / (t * 1e-3) for p, t in train.items()},
                              **{f"{p}_ms_per_step": t for p, t in train.items()},
-                             "speedup_fp16_vs_fp32": train["fp32"] / train["fp16"]},
+                             "speedup_fp16_vs_fp32": train["fp32"] / train["fp16"],
+                             "roofline": roof("tensor", TRAIN_FLOP_PER_SAMPLE * nt, train["fp16"],
+                                              f"fwd + bwd FLOPs of the FP16 step; Adam moves 33 B x {vis_train_params} params "
+                                              f"= {33 * vis_train_params / 1e6:.1f} MB per step; the fused kernel is bound by the "
+                                              "L2 reduction rate of the grid-gradient scatter")},
         "throughput_train": {"batch": ntt, "unit": "samples/s", "flop_per_sample": 3 * FLOP_PER_QUERY,
                              "optimizer": "Ema(0.95) of ExponentialDecay(Adam lr 5e-3)", "loss": "RelativeL2",
                              **{f"{p}_samples_per_s": ntt / (t * 1e-3) for p, t in ttrain.items()},
                              **{f"{p}_ms_per_step": t for p, t in ttrain.items()},
-                             "speedup_fp16_vs_fp32": ttrain["fp32"] / ttrain["fp16"]},
+                             "speedup_fp16_vs_fp32": ttrain["fp32"] / ttrain["fp16"],
+                             "roofline": roof("tensor", 3 * FLOP_PER_QUERY * ntt, ttrain["fp16"],
+                                              f"fwd + bwd FLOPs of the FP16 step; Adam + EMA move about 41 B x {thr_train_params} "
+                                              "params per step; bound by the L2 reduction rate of the grid-gradient scatter")},
         "render": {"workload": "1024x1024 pinhole rays, level 3 (64^3) of a 512^3->4^3 pyramid (256^3 value noise, "
                                "30% occupied, upsampled x2), 4 path vertices, <= 64 visibility queries per bounce",
                    "frame": "one CUDA-graph launch: the persistent kernel (fp16) or rounds in a conditional while node "
                             "(fp16_wavefront, fp32)", **render,
+                   "roofline": {k: roof("tensor", render_flop[k], v["p50_ms"], "12,416 FLOP per visibility query + 34,176 per "
+                                        "throughput query over the p50 frame") for k, v in render.items()},
                    "cpu_queries_per_s": (rtot[0] + rtot[1]) / cpu_render_s,
                    "cpu_sample": "96x96 rays of the same camera, FP64 host restatement, all host threads"},
         "sample_generator": generator,
         "voxelize": {"triangles": 2_000_000, "grid": 1024, "ms": tvox, "triangles_per_s": 2e6 / (tvox * 1e-3),
-                     "scene": "20k ellipsoid shells (48 tris) + 0.52M quads, unit cube, 1e-4 padding"},
+                     "scene": "20k ellipsoid shells (48 tris) + 0.52M quads, unit cube, 1e-4 padding",
+                     "roofline": roof("hbm", 36 * 2_000_000 + (1 << 27), tvox, "36 B per triangle read + the 128 MiB grid "
+                                      "written once; the kernel is instruction-issue bound (per-voxel overlap tests)")},
         "voxelize_train": {"pyramid_ms": t_pyr * 1e3, "batch": n4, "batches": n_batches, **e2e4,
                            "targets": "albedo(voxel centre) x exact-DDA transmittance along wi, LoD 0-7 of the 1024^3 pyramid",
                            "loss": "RelativeL2", "optimizer": "Ema(0.95) of ExponentialDecay(Adam lr 5e-3)"},

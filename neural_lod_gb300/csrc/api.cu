@@ -1015,7 +1015,7 @@ int nlod_set_kernel_variant(nlod_module* m, int variant) {
             if (variant != 0) throw Error(NLOD_ERR_INVALID, "the FP32 form has a single kernel variant");
             return;
         }
-        if (!tc_variant_ok(m->d, variant)) throw Error(NLOD_ERR_UNSUPPORTED, "kernel variant does not fit this network");
+        if (!tc_variant_ok(m->d, variant, m->op_kind())) throw Error(NLOD_ERR_UNSUPPORTED, "kernel variant does not fit this network");
         m->tc_variant = variant;
     });
 }
@@ -1037,7 +1037,7 @@ int nlod_autotune(nlod_module* m, void* stream, uint32_t n, const float* in, flo
         ForwardArgs a = base_forward_args(m, n, in, true);
         a.out = out;
         for (int v = 0; v < tc_num_variants(); ++v) {
-            if (!tc_variant_ok(m->d, v)) continue;
+            if (!tc_variant_ok(m->d, v, m->op_kind())) continue;
             cuda_check(launch_forward_tc(m->d, a, m->op_kind(), v, m->status, s), "autotune");
             cuda_check(cudaEventRecord(e0, s), "event");
             for (int it = 0; it < 3; ++it) cuda_check(launch_forward_tc(m->d, a, m->op_kind(), v, m->status, s), "autotune");

@@ -164,7 +164,7 @@ __device__ __forceinline__ void table_quad(const __half* t, uint32_t a, uint32_t
 template <int NL, typename TT = float>
 __device__ __forceinline__ void grid_group_forward(const GridDesc& g, const GridLevel* __restrict__ levels, uint32_t l0, uint32_t nl,
                                                    const TT* __restrict__ table, float px, float py, float pz, float ml_frac,
-                                                   float (&f)[2 * NL]) {
+                                                   float (&f)[2 * NL], const uint32_t* smem_tab = nullptr, uint32_t smem_levels = 0) {
     uint32_t p0, p1, p2;
     hash_primes(g.hash, p0, p1, p2);
     float2 v[NL][8];
@@ -199,6 +199,14 @@ __device__ __forceinline__ void grid_group_forward(const GridDesc& g, const Grid
                 for (int c = 0; c < 8; c += 2) {
                     const uint32_t ea = e[c], eb = e[c + 1];
                     if constexpr (std::is_same<TT, __half>::value) {
+                        if (l < smem_levels) {
+                            // a level staged in shared memory: one FP16 pair per 32-bit word
+                            const uint32_t* sl = smem_tab + L.offset;
+                            const uint32_t wa = sl[ea], wb = sl[eb];
+                            v[i][c] = __half22float2(*reinterpret_cast<const __half2*>(&wa));
+                            v[i][c + 1] = __half22float2(*reinterpret_cast<const __half2*>(&wb));
+                            continue;
+                        }
                         if ((ea >> 2) == (eb >> 2)) {
                             table_quad(lv, ea, eb, v[i][c], v[i][c + 1]);
                         } else {
@@ -425,7 +433,8 @@ __device__ __forceinline__ void encode_slot_scalar(const Slot& s, const ModelDes
 template <int NL, typename Store, typename TT = float>
 __device__ __forceinline__ void encode_tile_rows(const ModelDesc& d, const GridLevel* level_tables, const TT* __restrict__ params,
                                                  const float* in_s, uint32_t in_ld, const float* __restrict__ ml_gpu, float ml_scalar,
-                                                 uint32_t row0, uint32_t rows, uint32_t tid, uint32_t nthreads, Store& st) {
+                                                 uint32_t row0, uint32_t rows, uint32_t tid, uint32_t nthreads, Store& st,
+                                                 const uint32_t* smem_tab = nullptr, uint32_t smem_levels = 0) {
     for (uint32_t r = tid; r < rows; r += nthreads) {
         const float* row = in_s + r * in_ld;
         const float ml = ml_gpu ? __ldg(ml_gpu + row0 + r) : ml_scalar;
@@ -441,7 +450,8 @@ __device__ __forceinline__ void encode_tile_rows(const ModelDesc& d, const GridL
                 for (uint32_t l0 = 0; l0 < nlev; l0 += NL) {
                     float f[2 * NL];
                     const uint32_t nl = min((uint32_t)NL, nlev - l0);
-                    grid_group_forward<NL, TT>(g, lv, l0, nl, table, px, py, pz, ml, f);
+                    // the staged levels belong to the first grid
+                    grid_group_forward<NL, TT>(g, lv, l0, nl, table, px, py, pz, ml, f, smem_tab, s.grid == 0 ? smem_levels : 0u);
                     st.run(r, s.out_begin + 2u * l0, f, 2u * nl);
                 }
                 if (s.n_pad) encode_slot_scalar(s, d, row, [&](uint32_t col, float v) { st.one(r, col, v); });

@@ -151,7 +151,9 @@ cudaError_t noalloc_scratch(void** ptr, size_t* bytes);
 // organisation (tile pipelines per CTA, grid levels per gather unit); see tc.cu.
 bool tc_supported(const ModelDesc& d);
 int tc_num_variants();
-bool tc_variant_ok(const ModelDesc& d, int variant);
+// kind: operand type of the module (1 = FP16, 2 = BF16); the variants that stage grid levels in
+// shared memory read the FP16 copy of the tables and exist for the FP16 form only.
+bool tc_variant_ok(const ModelDesc& d, int variant, int kind = 1);
 int tc_default_variant(const ModelDesc& d);
 cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, int variant, uint32_t* status, cudaStream_t s);
 

@@ -532,7 +532,8 @@ __global__ void __launch_bounds__(2 * kGroupThreads + MW * 32, 1)
             for (int k = 0; k < K; ++k) mine_empty &= ld_state(&state[mlane + (uint32_t)k * (MW * 32)]) == WS_EMPTY;
             if (__all_sync(kFull, queue_done && mine_empty)) break;
             if (!__any_sync(kFull, progress)) {
-                if ((it & 63u) == 0 && globaltimer_ns() - t_start > kFrameNs) {
+                // the time bound is decided for the whole warp, so that no lane leaves alone
+                if ((it & 63u) == 0 && __any_sync(kFull, globaltimer_ns() - t_start > kFrameNs)) {
                     if (lane == 0) atomicOr(A.status, 4u);
                     break;
                 }
@@ -556,7 +557,7 @@ __global__ void __launch_bounds__(2 * kGroupThreads + MW * 32, 1)
         uint64_t* bar = &bars[grp];
         uint32_t* vis_rows = reinterpret_cast<uint32_t*>(smem + L.rows) + grp * (2u * 128u + 4u);
         uint32_t* thr_rows = vis_rows + 128;
-        uint32_t* cnt = vis_rows + 256;                     // [0] visibility, [1] throughput ready
+        uint32_t* cnt = vis_rows + 256;                     // [0] visibility, [1] throughput ready, [2] active marchers
         const TT* vtab = static_cast<const TT*>(A.vis.table);
         const TT* ttab = static_cast<const TT*>(A.thr.table);
         const uint32_t first = grp * kHalf;
@@ -566,12 +567,16 @@ __global__ void __launch_bounds__(2 * kGroupThreads + MW * 32, 1)
         uint32_t waited = 0, passes = 0;
         for (uint32_t it = 0;; ++it) {
             // ---- collect the ready slots of this group's half ----
+            // Every decision below is taken on values the whole group reads after a group
+            // barrier (one thread samples the marcher count), so no thread of the group leaves the
+            // loop or skips a pass alone: the group barriers have 128 arrivals on every path.
             if (gtid == 0) {
                 cnt[0] = 0u;
                 cnt[1] = 0u;
+                cnt[2] = ld_state(active_marchers);
             }
-            const bool marchers_gone = ld_state(active_marchers) == 0u;
             group_sync(bar_id);
+            const bool marchers_gone = cnt[2] == 0u;
             for (uint32_t j = gtid; j < kHalf; j += kGroupThreads) {
                 const uint32_t s = first + j;
                 const uint32_t v = ld_state(&state[s]);

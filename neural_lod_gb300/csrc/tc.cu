@@ -48,14 +48,16 @@ struct TcLayout {
     uint32_t in_ld;
     uint32_t group_stride;
     uint32_t lvl_off;             // grid level tables (kMaxGrids x kMaxLevels GridLevel)
-    uint32_t bar_off;             // G mbarriers, then the TMEM base address
+    uint32_t bar_off;             // G + 1 mbarriers (the last for the staged levels), then the TMEM base address
     uint32_t total;
     uint32_t tmem_cols;           // G * width rounded up to a power of two
+    uint32_t tab_off, tab_bytes;  // leading levels of the first grid staged in shared memory (FP16)
+    uint32_t tab_levels;
 };
 
 __host__ __device__ inline uint32_t align_up(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
 
-__host__ __device__ inline TcLayout tc_layout(const ModelDesc& d, int G) {
+__host__ __device__ inline TcLayout tc_layout(const ModelDesc& d, int G, bool stage_levels = false) {
     TcLayout L{};
     uint32_t off = align_up(d.n_params_network * 2u, 128);
     L.w_bytes = off;
@@ -67,8 +69,26 @@ __host__ __device__ inline TcLayout tc_layout(const ModelDesc& d, int G) {
     off += (uint32_t)G * L.group_stride;
     L.lvl_off = off;
     off += kMaxGrids * kMaxLevels * (uint32_t)sizeof(GridLevel);
+    if (stage_levels && d.n_grids > 0 && d.grids[0].interp != INTERP_NEAREST && d.grids[0].n_features == 2) {
+        // as many leading levels of the first grid (4 bytes per FP16 entry pair) as fit in what is
+        // left of the 227 KB a CTA may use
+        const uint32_t tab_off = align_up(off, 128);
+        const uint32_t tail = 8u * (uint32_t)G + 16u + 256u;
+        const uint32_t room = 227u * 1024u > tab_off + tail ? 227u * 1024u - tab_off - tail : 0u;
+        const GridDesc& g = d.grids[0];
+        for (uint32_t l = 0; l < g.n_levels; ++l) {
+            const uint32_t end = (g.levels[l].offset + g.levels[l].size) * 4u;
+            if (end > room) break;
+            L.tab_levels = l + 1;
+            L.tab_bytes = end;
+        }
+        if (L.tab_levels) {
+            L.tab_off = tab_off;
+            off = tab_off + L.tab_bytes;
+        }
+    }
     L.bar_off = off;
-    off += 8 * G + 8;
+    off += 8 * G + 16;
     L.total = align_up(off, 128);
     uint32_t cols = 32;
     while (cols < (uint32_t)G * d.width) cols <<= 1;   // TMEM allocations are powers of two
@@ -76,16 +96,18 @@ __host__ __device__ inline TcLayout tc_layout(const ModelDesc& d, int G) {
     return L;
 }
 
-template <int W, typename T, int G, int NL>
+template <int W, typename T, int G, int NL, bool ST>
 __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward_tc(const __grid_constant__ ModelDesc d,
                                                                                     const __grid_constant__ ForwardArgs a,
                                                                                     uint32_t* __restrict__ status) {
     using Op = tc::OpType<T>;
     constexpr int kThreads = G * kGroupThreads;
     extern __shared__ __align__(1024) uint8_t smem[];
-    const TcLayout L = tc_layout(d, G);
+    // ST: the first grid's leading levels are staged in shared memory (FP16 form), so their
+    // gathers are shared-memory loads instead of L1/L2 requests
+    const TcLayout L = tc_layout(d, G, ST && std::is_same<T, __half>::value);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L.bar_off);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 8 * G);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L.bar_off + 8 * G + 8);
 
     const uint32_t tid = threadIdx.x;
     const uint32_t warp = tid >> 5, lane = tid & 31;
@@ -117,8 +139,15 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
 
     // ---- set-up: barriers, TMEM, resident weights ----
     if (tid == 0) {
-        for (int g = 0; g < G; ++g) tc::mbar_init(&bars[g], 1);
+        for (int g = 0; g <= G; ++g) tc::mbar_init(&bars[g], 1);
         tc::fence_barrier_init();
+        if (L.tab_levels) {
+            // one bulk copy of the staged levels (16-byte aligned: the grid starts on a 512-byte
+            // boundary of the FP16 copy, levels on multiples of 8 entries)
+            const uint8_t* src = static_cast<const uint8_t*>(a.grid_h) + 2u * d.grids[0].param_offset;
+            tc::mbar_arrive_expect_tx(&bars[G], L.tab_bytes);
+            tc::bulk_copy_g2s(smem + L.tab_off, src, L.tab_bytes, &bars[G]);
+        }
     }
     if (warp == 0) {
         tc::tmem_alloc(tmem_slot, L.tmem_cols);
@@ -147,6 +176,10 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    bool aborted = false;
+    if (L.tab_levels && !tc::mbar_wait_bounded(&bars[G], 0, kWaitCycles)) aborted = true;
+    aborted = __syncthreads_or(aborted);
+    const uint32_t* tab_s = reinterpret_cast<const uint32_t*>(smem + L.tab_off);
     const uint32_t tmem_base = *tmem_slot + grp * (uint32_t)W;
     uint8_t* a_tile = smem + L.w_bytes + grp * L.group_stride;
     float* in_s = reinterpret_cast<float*>(a_tile + L.in_rel);
@@ -154,8 +187,7 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
     const uint32_t a_addr = tc::smem_addr(a_tile);
 
     uint32_t phase = 0;
-    bool aborted = false;
-    const uint32_t n_tiles = forward_rows(a) / kTcTile;
+    const uint32_t n_tiles = aborted ? 0u : forward_rows(a) / kTcTile;
     const uint32_t row = quarter * 32u + lane;   // TMEM lane == tile row owned in the epilogue
     const uint32_t taddr_row = tmem_base + ((quarter * 32u) << 16);
 
@@ -176,7 +208,7 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
             // entry, tiny-cuda-nn's half-precision parameters), the BF16 form from the FP32 tables
             if constexpr (std::is_same<T, __half>::value)
                 encode_tile_rows<NL>(d, lvl_s, static_cast<const __half*>(a.grid_h), in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile,
-                                     gtid, kGroupThreads, st);
+                                     gtid, kGroupThreads, st, tab_s, L.tab_levels);
             else
                 encode_tile_rows<NL>(d, lvl_s, a.params, in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile, gtid, kGroupThreads, st);
         }
@@ -255,8 +287,10 @@ __global__ void __launch_bounds__(G * kGroupThreads, (G == 2 ? 2 : 1)) k_forward
 
     // ---- teardown ----
     if (aborted) {
-        // Give the group's outstanding MMAs one more bounded chance to finish before TMEM is released.
+        // Give the group's outstanding MMAs (and the staging copy) one more bounded chance to
+        // finish before TMEM and shared memory are released.
         (void)tc::mbar_wait_bounded(bar, phase ^ 1u, kWaitCycles);
+        if (L.tab_levels) (void)tc::mbar_wait_bounded(&bars[G], 0, kWaitCycles);
         if (gtid == 0) atomicOr(status, 1u);
     }
     tc::fence_before_sync();
@@ -280,8 +314,8 @@ int sm_count() {
 
 // Dynamic shared memory request: what the tiles need, raised so that TMEM (512 columns per SM)
 // can never be over-subscribed by co-resident CTAs.
-size_t tc_smem_bytes(const ModelDesc& d, int G, int* per_sm_out) {
-    const TcLayout L = tc_layout(d, G);
+size_t tc_smem_bytes(const ModelDesc& d, int G, bool stage_levels, int* per_sm_out) {
+    const TcLayout L = tc_layout(d, G, stage_levels);
     const uint32_t cap = 512u / L.tmem_cols;               // CTAs whose TMEM fits on one SM
     const size_t sm_bytes = 233472;                        // 228 KB per SM
     size_t bytes = L.total;
@@ -297,23 +331,25 @@ size_t tc_smem_bytes(const ModelDesc& d, int G, int* per_sm_out) {
 
 struct Variant {
     int G, NL;
+    bool stage_levels;
 };
-constexpr Variant kVariants[] = {{2, 2}, {2, 4}, {4, 2}, {4, 4}, {6, 2}, {5, 2}, {6, 1}};
+constexpr Variant kVariants[] = {{2, 2, false}, {2, 4, false}, {4, 2, false}, {4, 4, false}, {6, 2, false}, {5, 2, false},
+                                 {6, 1, false}, {4, 2, true}, {4, 1, true}, {6, 1, true}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-template <int W, typename T, int G, int NL>
+template <int W, typename T, int G, int NL, bool ST = false>
 cudaError_t launch_variant(const ModelDesc& d, const ForwardArgs& a, uint32_t* status, cudaStream_t s) {
     int per_sm = 1;
-    const size_t bytes = tc_smem_bytes(d, G, &per_sm);
+    const size_t bytes = tc_smem_bytes(d, G, ST && std::is_same<T, __half>::value, &per_sm);
     if (bytes > 227u * 1024u || per_sm < 1) return cudaErrorInvalidConfiguration;
     const uint32_t n_tiles = a.n / kTcTile;
     uint32_t blocks = (uint32_t)(per_sm * sm_count());
     const uint32_t need = (n_tiles + G - 1) / G;
     if (blocks > need) blocks = need;
     if (blocks == 0) return cudaSuccess;
-    cudaError_t e = ensure_dynamic_smem((const void*)k_forward_tc<W, T, G, NL>, bytes);
+    cudaError_t e = ensure_dynamic_smem((const void*)k_forward_tc<W, T, G, NL, ST>, bytes);
     if (e != cudaSuccess) return e;
-    k_forward_tc<W, T, G, NL><<<blocks, G * kGroupThreads, bytes, s>>>(d, a, status);
+    k_forward_tc<W, T, G, NL, ST><<<blocks, G * kGroupThreads, bytes, s>>>(d, a, status);
     return cudaGetLastError();
 }
 
@@ -327,6 +363,10 @@ cudaError_t launch_typed(const ModelDesc& d, const ForwardArgs& a, int variant, 
         case 4: return launch_variant<W, T, 6, 2>(d, a, status, s);
         case 5: return launch_variant<W, T, 5, 2>(d, a, status, s);
         case 6: return launch_variant<W, T, 6, 1>(d, a, status, s);
+        // the staging variants exist for the FP16 form (its grid tables have an FP16 copy)
+        case 7: return std::is_same<T, __half>::value ? launch_variant<W, T, 4, 2, true>(d, a, status, s) : cudaErrorInvalidValue;
+        case 8: return std::is_same<T, __half>::value ? launch_variant<W, T, 4, 1, true>(d, a, status, s) : cudaErrorInvalidValue;
+        case 9: return std::is_same<T, __half>::value ? launch_variant<W, T, 6, 1, true>(d, a, status, s) : cudaErrorInvalidValue;
         default: return cudaErrorInvalidValue;
     }
 }
@@ -335,10 +375,12 @@ cudaError_t launch_typed(const ModelDesc& d, const ForwardArgs& a, int variant, 
 
 int tc_num_variants() { return kNumVariants; }
 
-bool tc_variant_ok(const ModelDesc& d, int variant) {
+bool tc_variant_ok(const ModelDesc& d, int variant, int kind) {
     if (variant < 0 || variant >= kNumVariants) return false;
+    if (kVariants[variant].stage_levels && kind != 1) return false;
     int per_sm = 0;
-    const size_t bytes = tc_smem_bytes(d, kVariants[variant].G, &per_sm);
+    const size_t bytes = tc_smem_bytes(d, kVariants[variant].G, kVariants[variant].stage_levels, &per_sm);
+    if (kVariants[variant].stage_levels && tc_layout(d, kVariants[variant].G, true).tab_levels == 0) return false;
     return bytes <= 227u * 1024u && per_sm >= 1 && (uint32_t)kVariants[variant].G * d.width <= 512u;
 }
 
@@ -355,7 +397,7 @@ bool tc_supported(const ModelDesc& d) {
 }
 
 cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, int variant, uint32_t* status, cudaStream_t s) {
-    if (!tc_variant_ok(d, variant)) return cudaErrorInvalidValue;
+    if (!tc_variant_ok(d, variant, kind)) return cudaErrorInvalidValue;
     if (kind == 1 && d.n_grids > 0 && !a.grid_h) return cudaErrorInvalidValue;   // the FP16 form reads the FP16 grid copy
     if (d.width == 64 && kind == 1) return launch_typed<64, __half>(d, a, variant, status, s);
     if (d.width == 64 && kind == 2) return launch_typed<64, __nv_bfloat16>(d, a, variant, status, s);

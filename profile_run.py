@@ -48,6 +48,23 @@ def main():
         if a.variant >= 0:
             m.kernel_variant = a.variant
         elif a.precision != "fp32":
+            # every variant's median time, L2 flushed before each launch, then the autotuner's pick
+            flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+            for v in range(m.n_kernel_variants):
+                try:
+                    m.kernel_variant = v
+                except N.NlodError:
+                    continue
+                ts = []
+                for _ in range(7):
+                    flush.fill_(1)
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    m.inference(x, out)
+                    e1.record()
+                    e1.synchronize()
+                    ts.append(e0.elapsed_time(e1))
+                print(f"variant {v}: {sorted(ts)[3]:.4f} ms")
             m.autotune(x, out)
         print("variant", m.kernel_variant)
         for _ in range(a.iters):
