@@ -1,8 +1,13 @@
 // Conservative surface voxelization: the triangle/voxel overlap test of cuda_voxelizer's
-// voxelize_triangle (cuda_voxelizer/src/voxelize.cu:58-190) with glm 0.9.9.8 vector arithmetic,
-// evaluated with one IEEE rounding per operation (no contraction: __fmul_rn / __fadd_rn /
-// __fsub_rn / __fdiv_rn / __fsqrt_rn), so that the voxel set is bit-exact with the same
-// arithmetic on the host.
+// voxelize_triangle (cuda_voxelizer/src/voxelize.cu:58-190) with glm 0.9.9.8 vector expressions
+// and the fused multiply-adds that nvcc's default contraction puts into that kernel (the
+// reference's build passes no -fmad flag).  Every operation is written with its rounding
+// (__fmaf_rn / __fmul_rn / __fadd_rn / __fsub_rn / __fdiv_rn / __fsqrt_rn), so the voxel set is
+// bit-exact with the reference kernel as built, and with the same arithmetic on the host:
+//   per triangle  cross: fma(a.y, b.z, -(b.y*a.z)) ...; dot3: fma(a.z, b.z, fma(a.x, b.x, a.y*b.y));
+//                 edge offsets: -1 * fma(n1, v_b, n0*v_a)
+//   per voxel     n.p: fma(n.x, p.x, n.y*p.y) + n.z*p.z; XY and YZ edge tests: fma(n0, p_a, n1*p_b)
+//                 + d; ZX edge tests: fma(n1, p.x, n0*p.z) + d.
 //
 // Work split.  The reference runs one thread per triangle and loops over the triangle's
 // candidate box, so one large triangle stalls its warp.  Here a warp stages 32 triangles in shared
@@ -24,9 +29,8 @@ constexpr int kVoxThreads = 256;
 __device__ __forceinline__ float gmin(float a, float b) { return (b < a) ? b : a; }
 __device__ __forceinline__ float gmax(float a, float b) { return (a < b) ? b : a; }
 __device__ __forceinline__ float dot3(float a0, float a1, float a2, float b0, float b1, float b2) {
-    return __fadd_rn(__fadd_rn(__fmul_rn(a0, b0), __fmul_rn(a1, b1)), __fmul_rn(a2, b2));
+    return __fmaf_rn(a2, b2, __fmaf_rn(a0, b0, __fmul_rn(a1, b1)));
 }
-__device__ __forceinline__ float dot2(float a0, float a1, float b0, float b1) { return __fadd_rn(__fmul_rn(a0, b0), __fmul_rn(a1, b1)); }
 
 // Everything the per-voxel test of one triangle needs.
 struct TriTest {
@@ -50,9 +54,9 @@ __device__ __forceinline__ void tri_setup(const float* T, const VoxFrame& f, Tri
         e[1][i] = __fsub_rn(v[2][i], v[1][i]);
         e[2][i] = __fsub_rn(v[0][i], v[2][i]);
     }
-    const float c0 = __fsub_rn(__fmul_rn(e[0][1], e[1][2]), __fmul_rn(e[1][1], e[0][2]));
-    const float c1 = __fsub_rn(__fmul_rn(e[0][2], e[1][0]), __fmul_rn(e[1][2], e[0][0]));
-    const float c2 = __fsub_rn(__fmul_rn(e[0][0], e[1][1]), __fmul_rn(e[1][0], e[0][1]));
+    const float c0 = __fmaf_rn(e[0][1], e[1][2], -__fmul_rn(e[1][1], e[0][2]));
+    const float c1 = __fmaf_rn(e[0][2], e[1][0], -__fmul_rn(e[1][2], e[0][0]));
+    const float c2 = __fmaf_rn(e[0][0], e[1][1], -__fmul_rn(e[1][0], e[0][1]));
     const float inv_len = __fdiv_rn(1.0f, __fsqrt_rn(dot3(c0, c1, c2, c0, c1, c2)));
     t.n[0] = __fmul_rn(c0, inv_len);
     t.n[1] = __fmul_rn(c1, inv_len);
@@ -90,7 +94,7 @@ __device__ __forceinline__ void tri_setup(const float* T, const VoxFrame& f, Tri
             }
             t.ne[pl][k][0] = n0;
             t.ne[pl][k][1] = n1;
-            t.de[pl][k] = __fadd_rn(__fadd_rn(__fmul_rn(-1.0f, dot2(n0, n1, v[k][a], v[k][b])), gmax(0.0f, __fmul_rn(f.unit[a], n0))),
+            t.de[pl][k] = __fadd_rn(__fadd_rn(__fmul_rn(-1.0f, __fmaf_rn(n1, v[k][b], __fmul_rn(n0, v[k][a]))), gmax(0.0f, __fmul_rn(f.unit[a], n0))),
                                     gmax(0.0f, __fmul_rn(f.unit[b], n1)));
         }
     }
@@ -99,14 +103,18 @@ __device__ __forceinline__ void tri_setup(const float* T, const VoxFrame& f, Tri
 // Overlap test of voxel (x, y, z) (grid indices) with the triangle.
 __device__ __forceinline__ bool tri_hits(const TriTest& t, const VoxFrame& f, int32_t x, int32_t y, int32_t z) {
     const float p[3] = {__fmul_rn((float)x, f.unit[0]), __fmul_rn((float)y, f.unit[1]), __fmul_rn((float)z, f.unit[2])};
-    const float nd = dot3(t.n[0], t.n[1], t.n[2], p[0], p[1], p[2]);
+    const float nd = __fadd_rn(__fmaf_rn(t.n[0], p[0], __fmul_rn(t.n[1], p[1])), __fmul_rn(t.n[2], p[2]));
     if (__fmul_rn(__fadd_rn(nd, t.d1), __fadd_rn(nd, t.d2)) > 0.0f) return false;
     bool ok = true;
 #pragma unroll
     for (int pl = 0; pl < 3; ++pl) {
         const int a = pl, b = (pl + 1) % 3;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) ok &= !(__fadd_rn(dot2(t.ne[pl][k][0], t.ne[pl][k][1], p[a], p[b]), t.de[pl][k]) < 0.0f);
+        for (int k = 0; k < 3; ++k) {
+            const float n0 = t.ne[pl][k][0], n1 = t.ne[pl][k][1];
+            const float s = pl == 2 ? __fmaf_rn(n1, p[b], __fmul_rn(n0, p[a])) : __fmaf_rn(n0, p[a], __fmul_rn(n1, p[b]));
+            ok &= !(__fadd_rn(s, t.de[pl][k]) < 0.0f);
+        }
     }
     return ok;
 }

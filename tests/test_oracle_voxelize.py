@@ -1,11 +1,13 @@
 """The voxelizer oracle (oracle/nlod_oracle.c: orc_mesh_frame, orc_voxelize) pinned by known
-answers and by an independent FP64 separating-axis overlap test.
+answers, by an independent FP64 separating-axis overlap test, and by the reference kernel's bits.
 
-The reference voxelizer ships no test or golden output and cannot be built here (it needs glm and
-trimesh2, neither of which is vendored), so these are the pins: the createMeshBBCube example of
-its own comment (cuda_voxelizer/src/util.h:77-85), hand-derived voxel sets, the MSB-first bit
-order of setBit (voxelize.cu:50-55), and agreement with the exact triangle/box overlap (13-axis
-separating-axis test in float64) everywhere except within rounding distance of a touching contact.
+The reference voxelizer ships no test or golden output.  Its kernel is compiled from its own source
+(oracle/build_ref.py, GLM from oracle/glm_shim) and run on a GPU to make
+tests/golden/voxelizer_golden.npz; the oracle must reproduce those bits exactly.  The other pins:
+the createMeshBBCube example of its own comment (cuda_voxelizer/src/util.h:77-85), hand-derived
+voxel sets, the MSB-first bit order of setBit (voxelize.cu:50-55), and agreement with the exact
+triangle/box overlap (13-axis separating-axis test in float64) everywhere except within rounding
+distance of a touching contact.
 """
 import numpy as np
 import pytest
@@ -127,3 +129,23 @@ def test_special_triangles(shape):
         tri = np.array([[3, 0.5, 0.5, 3, 2.5, 0.5, 3, 0.5, 2.5]], np.float32)
         got = _vox_set(oracle.voxelize(tri, g, [0, 0, 0], [1, 1, 1]), g)
         assert got and all(x == 3 for x, _, _ in got)
+
+
+def test_oracle_matches_reference_kernel_build():
+    """The host restatement against the reference voxelizer kernel itself, compiled from its source
+    the way the reference builds it (nvcc's default multiply-add contraction) and run on a GB300
+    (tests/golden/make_voxelizer_golden.py): the same bits on a 20,000-triangle soup at 100^3."""
+    import sys
+    from pathlib import Path
+
+    golden = Path(__file__).resolve().parent / "golden" / "voxelizer_golden.npz"
+    if not golden.exists():
+        pytest.skip("reference voxelizer golden vectors not generated")
+    sys.path.insert(0, str(golden.parent))
+    import make_voxelizer_golden as M
+
+    g = np.load(golden)
+    tris = M.soup(int(g["n"]), int(g["grid"]), int(g["seed"]))
+    got = oracle.voxelize(tris, int(g["grid"]), g["bbox_min"], g["unit"])
+    assert int(np.unpackbits(g["bits"].view(np.uint8)).sum()) > 100_000
+    assert np.array_equal(got, g["bits"])
