@@ -439,7 +439,7 @@ def main():
         mv.set_max_level_gpu(fracd)
         ov = torch.empty((nv, 1), device=dev)
         if prec != "fp32":
-            mv.autotune(xvd, ov)     # the kernel organisation for this batch size
+            vis["variant"] = mv.autotune(xvd, ov)     # the kernel organisation for this batch size
         tv = time_steps(lambda: mv.inference(xvd, ov), args.steps, 3, flush)
         vis[prec] = nv / (statistics.median(tv) * 1e-3)
         del mv
@@ -661,7 +661,8 @@ def main():
         "fp32_form": {"value": n / (ms32 * 1e-3), "unit": UNIT, "ms_per_step": ms32},
         "speedup_fp16_vs_fp32": ms32 / ms16,
         "err_vs_fp64": {"fp16_mean_abs": err16, "fp32_mean_abs": err32, "sample": ns},
-        "visibility_query": {"batch": nv, "fp16_queries_per_s": vis["fp16"], "fp32_queries_per_s": vis["fp32"]},
+        "visibility_query": {"batch": nv, "fp16_queries_per_s": vis["fp16"], "fp32_queries_per_s": vis["fp32"],
+                             "fp16_kernel_variant": vis["variant"]},
         "visibility_train": {"batch": nt, "unit": "samples/s", "flop_per_sample": TRAIN_FLOP_PER_SAMPLE,
                              **{f"{p}_samples_per_s": nt / (t * 1e-3) for p, t in train.items()},
                              **{f"{p}_ms_per_step": t for p, t in train.items()},

@@ -313,8 +313,10 @@ typedef struct nlod_render_params {
     float lod_max_level;           /* visibility network's max grid level fraction for this LoD */
     float lod_input;               /* throughput network's LoD input column for this LoD */
     uint64_t seed;                 /* direction sampling */
-    uint32_t mode;                 /* NLOD_RENDER_AUTO: the persistent kernel when both modules are tensor-core
-                                      modules of one operand type, else the wavefront rounds;
+    uint32_t mode;                 /* NLOD_RENDER_AUTO: when both modules are tensor-core modules of one
+                                      operand type, the faster of the persistent kernel (organisation
+                                      autotuned) and the wavefront rounds, timed on this scene at
+                                      creation; else the wavefront rounds.
                                       NLOD_RENDER_WAVEFRONT / NLOD_RENDER_PERSISTENT force one form */
 } nlod_render_params;
 

@@ -357,6 +357,37 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
                 cuda_check(e, "persistent frame graph");
                 cuda_check(e2, "persistent frame graph");
                 cuda_check(cudaGraphInstantiate(&r->exec, r->graph, 0), "graph instantiate");
+                if (p->mode == NLOD_RENDER_AUTO) {
+                    // The automatic choice also times the wavefront form on this scene and keeps
+                    // whichever frame is faster (one timed frame of each graph after a warm-up).
+                    nlod_render_params pw = *p;
+                    pw.mode = NLOD_RENDER_WAVEFRONT;
+                    nlod_renderer* wf = nullptr;
+                    if (nlod_renderer_create(visibility, throughput, grid, &pw, &wf) == NLOD_OK) {
+                        auto frame_ms = [&](cudaGraphExec_t x) {
+                            cudaEvent_t a0, a1;
+                            float ms = 3.0e38f;
+                            if (cudaEventCreate(&a0) != cudaSuccess) return ms;
+                            if (cudaEventCreate(&a1) == cudaSuccess) {
+                                if (cudaGraphLaunch(x, s) == cudaSuccess && cudaEventRecord(a0, s) == cudaSuccess &&
+                                    cudaGraphLaunch(x, s) == cudaSuccess && cudaEventRecord(a1, s) == cudaSuccess &&
+                                    cudaEventSynchronize(a1) == cudaSuccess)
+                                    cudaEventElapsedTime(&ms, a0, a1);
+                                cudaEventDestroy(a1);
+                            }
+                            cudaEventDestroy(a0);
+                            return ms;
+                        };
+                        const float ms_pk = frame_ms(r->exec), ms_wf = frame_ms(wf->exec);
+                        cuda_check(cudaStreamSynchronize(s), "synchronize");
+                        if (ms_wf < ms_pk) {
+                            nlod_renderer_destroy(r.release());
+                            *out = wf;
+                            return;
+                        }
+                        nlod_renderer_destroy(wf);
+                    }
+                }
                 *out = r.release();
                 return;
             }

@@ -6,8 +6,10 @@
 // bit-exact with the reference kernel as built, and with the same arithmetic on the host:
 //   per triangle  cross: fma(a.y, b.z, -(b.y*a.z)) ...; dot3: fma(a.z, b.z, fma(a.x, b.x, a.y*b.y));
 //                 edge offsets: -1 * fma(n1, v_b, n0*v_a)
-//   per voxel     n.p: fma(n.x, p.x, n.y*p.y) + n.z*p.z; XY and YZ edge tests: fma(n0, p_a, n1*p_b)
-//                 + d; ZX edge tests: fma(n1, p.x, n0*p.z) + d.
+//   per voxel     n.p: fma(n.x, p.x, n.y*p.y) + n.z*p.z, but (n.x*p.x + n.y*p.y) + n.z*p.z in the
+//                 first voxel of a row with an odd voxel count (the reference's x loop, unrolled by
+//                 two, runs that voxel on its own); XY and YZ edge tests: fma(n0, p_a, n1*p_b) + d;
+//                 ZX edge tests: fma(n1, p.x, n0*p.z) + d.
 //
 // Work split.  The reference runs one thread per triangle and loops over the triangle's
 // candidate box, so one large triangle stalls its warp.  Here a warp stages 32 triangles in shared
@@ -103,7 +105,12 @@ __device__ __forceinline__ void tri_setup(const float* T, const VoxFrame& f, Tri
 // Overlap test of voxel (x, y, z) (grid indices) with the triangle.
 __device__ __forceinline__ bool tri_hits(const TriTest& t, const VoxFrame& f, int32_t x, int32_t y, int32_t z) {
     const float p[3] = {__fmul_rn((float)x, f.unit[0]), __fmul_rn((float)y, f.unit[1]), __fmul_rn((float)z, f.unit[2])};
-    const float nd = __fadd_rn(__fmaf_rn(t.n[0], p[0], __fmul_rn(t.n[1], p[1])), __fmul_rn(t.n[2], p[2]));
+    // the reference build runs its x loop in pairs after one leading voxel when a row has an odd
+    // voxel count; that leading voxel's plane dot product rounds all three products
+    const bool lead = x == t.lo[0] && (t.ext[0] & 1);
+    const float nx = lead ? __fmul_rn(t.n[0], p[0]) : 0.0f;
+    const float nd = lead ? __fadd_rn(__fadd_rn(nx, __fmul_rn(t.n[1], p[1])), __fmul_rn(t.n[2], p[2]))
+                          : __fadd_rn(__fmaf_rn(t.n[0], p[0], __fmul_rn(t.n[1], p[1])), __fmul_rn(t.n[2], p[2]));
     if (__fmul_rn(__fadd_rn(nd, t.d1), __fadd_rn(nd, t.d2)) > 0.0f) return false;
     bool ok = true;
 #pragma unroll

@@ -689,12 +689,14 @@ int orc_first_active_voxel_clip(const OrcLodLevel* L, const float E[3], const fl
  * multiply-adds of the reference kernel as nvcc builds it by default (the reference's CMake passes
  * no -fmad flag).  Which products nvcc fuses was established by running that build, compiled from
  * its source, against candidate restatements (bit for bit on 4.8 M voxels of random triangle
- * soups at 100^3, 256^3 and 512^3):
+ * soups at 100^3, 256^3 and 512^3, and on the 82.4 M voxels of the 2.0 M-triangle scene at 1024^3):
  *   per triangle  cross: fma(a.y, b.z, -(b.y*a.z)) ...; dot3: fma(a.z, b.z, fma(a.x, b.x, a.y*b.y));
  *                 edge offsets: -1 * fma(n1, v_b, n0*v_a) (the product of the edge vector's negated
  *                 component is the one left unfused)
  *   per voxel     n.p: fma(n.x, p.x, n.y*p.y) + n.z*p.z (the products invariant over the innermost
- *                 x loop are computed apart); XY and YZ edge tests: fma(n0, p_a, n1*p_b) + d;
+ *                 x loop are computed apart), except (n.x*p.x + n.y*p.y) + n.z*p.z in the first
+ *                 voxel of a row with an odd voxel count (the x loop is unrolled by two and that
+ *                 voxel runs on its own); XY and YZ edge tests: fma(n0, p_a, n1*p_b) + d;
  *                 ZX edge tests: fma(n1, p.x, n0*p.z) + d.
  * Every other operation is rounded once (built with -ffp-contract=off; fmaf rounds once).
  * ------------------------------------------------------------------------------------------- */
@@ -768,7 +770,16 @@ void orc_voxelize(const float* tris, int64_t n, const float bmin[3], const float
             for (int y = lo[1]; y <= hi[1]; ++y)
                 for (int x = lo[0]; x <= hi[0]; ++x) {
                     const float p[3] = {(float)x * unit[0], (float)y * unit[1], (float)z * unit[2]};
-                    const float nd = fmaf(nrm[0], p[0], nrm[1] * p[1]) + nrm[2] * p[2];
+                    /* the reference build fuses n.x * p.x into the plane dot product, except in the
+                       first voxel of a row with an odd voxel count: its loop over x runs in pairs
+                       after that one, which rounds all three products */
+                    float nd;
+                    if (x == lo[0] && ((hi[0] - lo[0]) & 1) == 0) {
+                        const float px = nrm[0] * p[0], py = nrm[1] * p[1], pz = nrm[2] * p[2];
+                        nd = (px + py) + pz;
+                    } else {
+                        nd = fmaf(nrm[0], p[0], nrm[1] * p[1]) + nrm[2] * p[2];
+                    }
                     if ((nd + d1) * (nd + d2) > 0.0f) continue;
                     int ok = 1;
                     for (int pl = 0; pl < 3 && ok; ++pl) {

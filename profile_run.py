@@ -19,6 +19,34 @@ from pathlib import Path
 sys.path.insert(0, str(Path(__file__).resolve().parent))
 
 
+def pick_variant(N, m, x, out, a, dev):
+    """--variant, or every variant's median time per call (L2 flushed before each launch) and then
+    the autotuner's pick."""
+    import torch
+
+    if a.variant >= 0:
+        m.kernel_variant = a.variant
+    elif a.precision != "fp32":
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+        for v in range(m.n_kernel_variants):
+            try:
+                m.kernel_variant = v
+            except N.NlodError:
+                continue
+            ts = []
+            for _ in range(15):
+                flush.fill_(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                m.inference(x, out)
+                e1.record()
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            print(f"variant {v}: {sorted(ts)[7]:.4f} ms")
+        m.autotune(x, out)
+    print("variant", m.kernel_variant)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("what", choices=["query", "train", "train_thr", "visq", "render", "voxelize", "sampler"])
@@ -45,28 +73,7 @@ def main():
         m = N.NetworkWithInputEncoding(10, 3, enc, net, precision=a.precision)
         x = torch.from_numpy(W.throughput_inputs(n, seed=1)).to(dev)
         out = torch.empty((n, 3), device=dev)
-        if a.variant >= 0:
-            m.kernel_variant = a.variant
-        elif a.precision != "fp32":
-            # every variant's median time, L2 flushed before each launch, then the autotuner's pick
-            flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-            for v in range(m.n_kernel_variants):
-                try:
-                    m.kernel_variant = v
-                except N.NlodError:
-                    continue
-                ts = []
-                for _ in range(7):
-                    flush.fill_(1)
-                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    e0.record()
-                    m.inference(x, out)
-                    e1.record()
-                    e1.synchronize()
-                    ts.append(e0.elapsed_time(e1))
-                print(f"variant {v}: {sorted(ts)[3]:.4f} ms")
-            m.autotune(x, out)
-        print("variant", m.kernel_variant)
+        pick_variant(N, m, x, out, a, dev)
         for _ in range(a.iters):
             m.inference(x, out)
     elif a.what == "visq":
@@ -78,6 +85,7 @@ def main():
         f = torch.from_numpy(frac).to(dev)
         m.set_max_level_gpu(f)
         out = torch.empty((n, 1), device=dev)
+        pick_variant(N, m, x, out, a, dev)
         for _ in range(a.iters):
             m.inference(x, out)
     elif a.what == "render":
