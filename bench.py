@@ -549,10 +549,13 @@ def main():
         rv.set_params(rv_params)
         rt.set_params(rt_params)
         if prec != "fp32":
-            xa = torch.from_numpy(W.visibility_inputs(1 << 18, seed=6)[0]).to(dev)
-            rv.autotune(xa, torch.empty((1 << 18, 1), device=dev))
-            xb = torch.from_numpy(W.throughput_inputs(1 << 18, seed=6)).to(dev)
-            rt.autotune(xb, torch.empty((1 << 18, 3), device=dev))
+            # kernel organisations for the frame's large rounds (0.5-0.8 M visibility queries at the
+            # frame's max level; throughput lists are evaluated from 32 K rows up)
+            xa = torch.from_numpy(W.visibility_inputs(1 << 20, seed=6)[0]).to(dev)
+            rv.set_max_level(rparams.lod_max_level)
+            rv.autotune(xa, torch.empty((1 << 20, 1), device=dev))
+            xb = torch.from_numpy(W.throughput_inputs(1 << 16, seed=6)).to(dev)
+            rt.autotune(xb, torch.empty((1 << 16, 3), device=dev))
         rr = Renderer(rv, rt, pyr, RenderParams(**{**rparams.__dict__, "mode": MODE_WAVEFRONT}) if "wavefront" in form else rparams)
         frame = torch.empty((1024, 1024, 3), device=dev)
         ft = time_steps(lambda: rr.frame(frame), max(5, args.steps) if prec != "fp32" else 5, 3, flush)

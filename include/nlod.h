@@ -317,12 +317,18 @@ typedef struct nlod_render_params {
                                       operand type, the faster of the persistent kernel (organisation
                                       autotuned) and the wavefront rounds, timed on this scene at
                                       creation; else the wavefront rounds.
-                                      NLOD_RENDER_WAVEFRONT / NLOD_RENDER_PERSISTENT force one form */
+                                      NLOD_RENDER_WAVEFRONT / NLOD_RENDER_PERSISTENT force one form;
+                                      NLOD_RENDER_HOST_ROUNDS issues the wavefront rounds from the host */
 } nlod_render_params;
 
 #define NLOD_RENDER_AUTO 0
 #define NLOD_RENDER_WAVEFRONT 1
 #define NLOD_RENDER_PERSISTENT 2
+/* The wavefront rounds issued one by one from the host, which reads the list sizes after every
+ * round (the reference's wavefront loop synchronises with the host the same way): the same
+ * kernels and pixels as NLOD_RENDER_WAVEFRONT, without the graph, so that a profiler sees every
+ * launch.  nlod_render_frame then synchronises the stream. */
+#define NLOD_RENDER_HOST_ROUNDS 3
 /* The persistent form with one organisation forced instead of autotuned (tests and tuning):
  * f = 4 or 6 tile pipelines per CTA that march their own rays, or f = 8 or 16 marcher warps
  * feeding two tensor-core groups (warp-specialized). */
@@ -345,8 +351,9 @@ NLOD_API int nlod_render_frame(nlod_renderer* r, void* stream, float* image, uin
  * NLOD_ERR_TIMEOUT if a ray ran out of DDA steps, the frame hit its round or time bound, or a
  * tensor-core wait timed out. */
 NLOD_API int nlod_render_stats(nlod_renderer* r, void* stream, uint64_t* out4);
-/* The form the renderer runs: NLOD_RENDER_WAVEFRONT, or NLOD_RENDER_PERSISTENT_FORM(f) with the
- * persistent organisation the autotune (or the caller) chose. */
+/* The form the renderer runs: NLOD_RENDER_WAVEFRONT, NLOD_RENDER_HOST_ROUNDS, or
+ * NLOD_RENDER_PERSISTENT_FORM(f) with the persistent organisation the autotune (or the caller)
+ * chose. */
 NLOD_API int nlod_renderer_mode(const nlod_renderer* r);
 
 /* ---- Per-voxel visibility thresholds ----------------------------------------------------------

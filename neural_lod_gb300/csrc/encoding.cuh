@@ -473,6 +473,55 @@ __device__ __forceinline__ void encode_tile_rows(const ModelDesc& d, const GridL
     }
 }
 
+// One part of one row's encoding, for tiles that TPR threads encode per row: part p takes grid
+// levels [p * per, (p + 1) * per) of every grid slot (per = the grid's levels / TPR, rounded up
+// to NL), and the last part also the other slots and the grids' padding.  Every column is
+// computed exactly as encode_tile_rows computes it.
+template <int NL, int TPR, typename Store, typename TT>
+__device__ __forceinline__ void encode_row_part(const ModelDesc& d, const GridLevel* level_tables, const TT* __restrict__ params,
+                                                const float* in_s, uint32_t in_ld, const float* __restrict__ ml_gpu, float ml_scalar,
+                                                uint32_t row0, uint32_t r, uint32_t part, Store& st, const uint32_t* smem_tab = nullptr,
+                                                uint32_t smem_levels = 0) {
+    const float* row = in_s + r * in_ld;
+    const float ml = ml_gpu ? __ldg(ml_gpu + row0 + r) : ml_scalar;
+    const bool last = part == (uint32_t)(TPR - 1);
+    for (uint32_t si = 0; si < d.n_slots; ++si) {
+        const Slot& s = d.slots[si];
+        if (s.type == SLOT_GRID) {
+            const float px = row[s.in_begin], py = row[s.in_begin + 1], pz = row[s.in_begin + 2];
+            const GridDesc& g = d.grids[s.grid];
+            const uint32_t nlev = g.n_levels;
+            const uint32_t per = ((nlev + TPR - 1) / TPR + NL - 1) / NL * NL;
+            const uint32_t lb = part * per, le = min(nlev, lb + per);
+            const TT* table = params + g.param_offset;
+            const GridLevel* lv = level_tables + s.grid * kMaxLevels;
+#pragma unroll 1
+            for (uint32_t l0 = lb; l0 < le; l0 += NL) {
+                float f[2 * NL];
+                const uint32_t nl = min((uint32_t)NL, le - l0);
+                grid_group_forward<NL, TT>(g, lv, l0, nl, table, px, py, pz, ml, f, smem_tab, s.grid == 0 ? smem_levels : 0u);
+                st.run(r, s.out_begin + 2u * l0, f, 2u * nl);
+            }
+            if (last && s.n_pad) encode_slot_scalar(s, d, row, [&](uint32_t col, float v) { st.one(r, col, v); });
+        } else if (!last) {
+            continue;
+        } else if (s.type == SLOT_SH && s.degree == 4 && s.n_pad == 0 && (s.out_begin & 1u) == 0) {
+            float v[16];
+            sh_forward(4u, row[s.in_begin], row[s.in_begin + 1], row[s.in_begin + 2], [&](uint32_t i, float x) { v[i] = x; });
+            st.run(r, s.out_begin, v, 16u);
+        } else if (s.type == SLOT_ONEHOT && s.out_width <= 16u && (s.out_width & 1u) == 0 && (s.out_begin & 1u) == 0) {
+            float v[16];
+            int bin = (int)floorf(row[s.in_begin] * (float)s.n_bins);
+            bin = bin < 0 ? 0 : (bin >= (int)s.n_bins ? (int)s.n_bins - 1 : bin);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = j == bin ? 1.0f : 0.0f;
+            st.run(r, s.out_begin, v, s.out_width);
+        } else {
+            encode_slot_scalar(s, d, row, [&](uint32_t col, float v) { st.one(r, col, v); });
+        }
+    }
+}
+
 // Encodes `rows` staged input rows (in_s, row stride in_ld) into the consumer's tile; each grid
 // unit covers NL levels (NL = 2 or 4).
 // Store must provide: run(r, col, const float (&f)[2*NL], n) storing f[0..n) at columns

@@ -31,6 +31,23 @@ inline cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes) {
     return e;
 }
 
+// CTAs of `kernel` with `threads` threads and `bytes` of dynamic shared memory that fit on one SM
+// at once (registers, threads and shared memory; cudaOccupancyMaxActiveBlocksPerMultiprocessor),
+// computed once per (kernel, device, bytes).  0 on an error.
+inline int resident_blocks(const void* kernel, int threads, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<std::pair<const void*, int>, size_t>, int> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find({{kernel, dev}, bytes});
+    if (it != cache.end()) return it->second;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, bytes) != cudaSuccess) n = 0;
+    cache[{{kernel, dev}, bytes}] = n;
+    return n;
+}
+
 // Inputs shared by every forward-style launch.
 struct ForwardArgs {
     uint32_t n;                       // elements (multiple of 128)

@@ -103,7 +103,7 @@ __device__ __forceinline__ bool slab(const float (&o)[3], const float (&d)[3], c
     far_t = 1e20f;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        const float inv = __fdiv_rn(1.f, d[i]);
+        const float inv = __frcp_rn(d[i]);   // 1 / d, correctly rounded (the same value as 1.f / d)
         const float lo = (float)ijk[i], hi = __fadd_rn(lo, 1.0f);
         if (d[i] == 0.f) {
             if (o[i] < lo || o[i] > hi) return false;
@@ -123,7 +123,8 @@ __device__ __forceinline__ bool slab(const float (&o)[3], const float (&d)[3], c
 __device__ __forceinline__ int first_active_voxel(const LodLevelDev& L, const float (&E)[3], const float (&D)[3], float t_min, const int32_t (&prev)[3],
                                   int32_t (&out)[3], float& t_near, float& t_far, uint32_t budget, float t_max = FLT_MAX) {
     if (L.n_active == 0) return 0;
-    const float inv[3] = {__fdiv_rn(1.f, D[0]), __fdiv_rn(1.f, D[1]), __fdiv_rn(1.f, D[2])};
+    // 1 / D correctly rounded (__frcp_rn: the value of the IEEE division 1.f / D)
+    const float inv[3] = {__frcp_rn(D[0]), __frcp_rn(D[1]), __frcp_rn(D[2])};
     float t0 = t_min, t1 = t_max;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {

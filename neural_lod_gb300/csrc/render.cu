@@ -76,16 +76,23 @@ __device__ __forceinline__ uint32_t push(uint32_t* counter, bool want) {
 
 enum : int { ACT_NONE_ = 0, ACT_VIS = 1, ACT_THR = 2 };
 
+// Throughput lists shorter than this are carried over (k_round), at most this many rounds in a row.
+constexpr uint32_t kThrDeferBelow = 32768u;
+constexpr uint32_t kThrDeferRounds = 8u;
+
 // One round for every queued ray (first = true: ray generation, every pixel's ray).
 __global__ void __launch_bounds__(256) k_step(const __grid_constant__ RenderConsts C, RenderBufs B, int first) {
     const uint32_t round = first ? 0u : B.ctl->round;
     const uint32_t p = (round + 1u) & 1u, q = round & 1u;   // lists read / written
     const uint32_t nv = first ? C.n_rays : B.ctl->n_vis;
     const uint32_t total = first ? C.n_rays : nv + B.ctl->n_thr;
+    // the throughput list was not evaluated this round: its rays go unchanged into the next list
+    const bool thr_carried = !first && B.ctl->thr_rows == 0u;
     for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
         const uint32_t j = base + threadIdx.x;
         const bool valid = j < total;
         int act = ACT_NONE_;
+        bool carried = false;
         uint32_t ray = 0;
         RayState st;
         if (valid) {
@@ -108,8 +115,13 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ RenderCons
                 const uint32_t jj = j - nv;
                 ray = B.lists[(p * 2 + 1) * C.n_rays + jj];
                 st = B.rays[ray];
-                const float t[3] = {B.thr_out[3 * jj], B.thr_out[3 * jj + 1], B.thr_out[3 * jj + 2]};
-                march = thr_resolve(st, t);
+                if (thr_carried) {
+                    act = ACT_THR;
+                    carried = true;
+                } else {
+                    const float t[3] = {B.thr_out[3 * jj], B.thr_out[3 * jj + 1], B.thr_out[3 * jj + 2]};
+                    march = thr_resolve(st, t);
+                }
             }
             if (march) {
                 const int mr = ray_march(C, st, B.image + 3 * (size_t)ray);
@@ -127,7 +139,7 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ RenderCons
         } else if (act == ACT_THR) {
             B.lists[(q * 2 + 1) * C.n_rays + slot_t] = ray;
             thr_row(C, st, B.thr_in + 10 * (size_t)slot_t);
-            B.ray_stats[2 * ray + 1] += 1u;
+            if (!carried) B.ray_stats[2 * ray + 1] += 1u;
         }
         if (valid) B.rays[ray] = st;
     }
@@ -137,10 +149,18 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ RenderCons
 __global__ void k_round(Control* ctl, uint32_t max_rounds, uint32_t* status, cudaGraphConditionalHandle cond, int use_cond) {
     const uint32_t q = ctl->round & 1u;
     const uint32_t nv = ctl->cnt[q * 2 + 0], nt = ctl->cnt[q * 2 + 1];
+    // A short throughput list waits for more rows instead of paying a whole inference launch for a
+    // few of them (a launch costs about as much for one tile as for a few hundred): it is carried
+    // into the next round, at most kThrDeferRounds rounds in a row and only while visibility
+    // queries keep the rounds going.  A carried ray's state and queries are unchanged, so every
+    // ray takes the same steps; only the round it takes them in moves.
+    const bool defer = nt > 0u && nt < kThrDeferBelow && nv > 0u && ctl->thr_deferred < kThrDeferRounds;
     ctl->n_vis = nv;
     ctl->n_thr = nt;
+    ctl->thr_rows = defer ? 0u : nt;
+    ctl->thr_deferred = defer ? ctl->thr_deferred + 1u : 0u;
     ctl->tot_vis += nv;
-    ctl->tot_thr += nt;
+    ctl->tot_thr += defer ? 0u : nt;
     ctl->tot_rounds += 1;
     ctl->cnt[(q ^ 1u) * 2 + 0] = 0u;
     ctl->cnt[(q ^ 1u) * 2 + 1] = 0u;
@@ -172,6 +192,7 @@ struct nlod_renderer {
     float vis_max_level = 1000.f;
     int mode = NLOD_RENDER_WAVEFRONT;
     int pk_groups = 0;              // tile pipelines per CTA of the persistent form (autotuned)
+    unsigned step_blocks = 0;       // k_step grid of the wavefront forms
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -275,7 +296,7 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             C.seed_lo = (uint32_t)p->seed;
             C.seed_hi = (uint32_t)(p->seed >> 32);
             C.budget = 64u * (uint32_t)C.L.res + 4096u;
-            C.max_rounds = p->max_depth * (p->max_vis_queries + 2u) + 4u;
+            C.max_rounds = p->max_depth * (p->max_vis_queries + 2u + kThrDeferRounds) + 4u;
             r->vis_max_level = p->lod_max_level;
             const uint32_t n = C.n_rays;
             r->n_pad = (n + 127u) / 128u * 128u;
@@ -298,14 +319,16 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
                 if (!ok) throw Error(NLOD_ERR_UNSUPPORTED, "persistent organisation " + std::to_string(f) + " is not available for these modules");
                 candidates[0] = f;
                 n_candidates = 1;
-            } else if (p->mode != NLOD_RENDER_AUTO && p->mode != NLOD_RENDER_WAVEFRONT && p->mode != NLOD_RENDER_PERSISTENT) {
+            } else if (p->mode != NLOD_RENDER_AUTO && p->mode != NLOD_RENDER_WAVEFRONT && p->mode != NLOD_RENDER_PERSISTENT &&
+                       p->mode != NLOD_RENDER_HOST_ROUNDS) {
                 throw Error(NLOD_ERR_INVALID, "unknown render mode");
             }
-            if (n_candidates) groups = candidates[0];
-            if (p->mode != NLOD_RENDER_AUTO && p->mode != NLOD_RENDER_WAVEFRONT && !groups)
+            const bool wavefront = p->mode == NLOD_RENDER_WAVEFRONT || p->mode == NLOD_RENDER_HOST_ROUNDS;
+            if (n_candidates && !wavefront) groups = candidates[0];
+            if (p->mode != NLOD_RENDER_AUTO && !wavefront && !groups)
                 throw Error(NLOD_ERR_UNSUPPORTED, "the persistent form needs two tensor-core modules of one operand type with "
                                                   "64-wide networks of 6 and 10 inputs");
-            if (p->mode != NLOD_RENDER_WAVEFRONT && groups) {
+            if (!wavefront && groups) {
                 auto alloc = [&](size_t bytes) {
                     void* q = dev_alloc<uint8_t>(bytes);
                     r->owned.push_back(q);
@@ -413,11 +436,13 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             // One launch of each inference with zero rows (outside any capture): sets the kernels'
             // shared-memory attributes before the graph is recorded.
             cuda_check(module_inference_device_count(r->vis, r->n_pad, B.vis_in, B.vis_out, &B.ctl->n_vis, r->vis_max_level, s), "inference");
-            cuda_check(module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->n_thr, 1000.f, s), "inference");
+            cuda_check(module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, s), "inference");
             cuda_check(cudaStreamSynchronize(s), "synchronize");
 
             // ---- the frame graph: reset, ray generation, then rounds in a conditional while node ----
             const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 152ull * 8);
+            r->step_blocks = blocks;
+            if (p->mode == NLOD_RENDER_HOST_ROUNDS) r->mode = NLOD_RENDER_HOST_ROUNDS;
             cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
             k_reset<<<1, 1, 0, s>>>(B.ctl);
             k_step<<<blocks, 256, 0, s>>>(C, B, 1);
@@ -443,7 +468,7 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             cudaError_t e = cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
                 e = module_inference_device_count(r->vis, r->n_pad, B.vis_in, B.vis_out, &B.ctl->n_vis, r->vis_max_level, bs);
-                if (e == cudaSuccess) e = module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->n_thr, 1000.f, bs);
+                if (e == cudaSuccess) e = module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, bs);
                 if (e == cudaSuccess) {
                     k_step<<<blocks, 256, 0, bs>>>(C, B, 0);
                     k_round<<<1, 1, 0, bs>>>(B.ctl, C.max_rounds, B.status, cond, 1);
@@ -472,7 +497,28 @@ int nlod_render_frame(nlod_renderer* r, void* stream, float* image, uint32_t* ra
     return guarded([&] {
         if (!r) throw Error(NLOD_ERR_INVALID, "renderer is NULL");
         cudaStream_t s = (cudaStream_t)stream;
-        cuda_check(cudaGraphLaunch(r->exec, s), "graph launch");
+        if (r->mode == NLOD_RENDER_HOST_ROUNDS) {
+            // the graph's rounds, issued from the host: it reads the list sizes after each round
+            RenderBufs& B = r->B;
+            const RenderConsts& C = r->C;
+            k_reset<<<1, 1, 0, s>>>(B.ctl);
+            k_step<<<r->step_blocks, 256, 0, s>>>(C, B, 1);
+            k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, B.status, 0, 0);
+            cuda_check(cudaGetLastError(), "launch");
+            for (;;) {
+                Control c;
+                cuda_check(cudaMemcpyAsync(&c, B.ctl, sizeof c, cudaMemcpyDeviceToHost, s), "copy");
+                cuda_check(cudaStreamSynchronize(s), "synchronize");
+                if (c.n_vis + c.n_thr == 0 || c.round > C.max_rounds) break;
+                cuda_check(module_inference_device_count(r->vis, r->n_pad, B.vis_in, B.vis_out, &B.ctl->n_vis, r->vis_max_level, s), "inference");
+                cuda_check(module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, s), "inference");
+                k_step<<<r->step_blocks, 256, 0, s>>>(C, B, 0);
+                k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, B.status, 0, 0);
+                cuda_check(cudaGetLastError(), "launch");
+            }
+        } else {
+            cuda_check(cudaGraphLaunch(r->exec, s), "graph launch");
+        }
         if (image)
             cuda_check(cudaMemcpyAsync(image, r->B.image, sizeof(float) * 3 * (size_t)r->C.n_rays, cudaMemcpyDeviceToDevice, s), "copy image");
         if (ray_stats)

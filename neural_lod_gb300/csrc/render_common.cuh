@@ -55,13 +55,16 @@ struct RenderConsts {
 };
 
 // Control words: [0..3] list counters [parity * 2 + kind] (the persistent form uses [0] as its
-// ray queue), [4] visibility rows, [5] throughput rows of the current round, [6] round, [7] rays
-// dropped at the per-bounce query cap; then 64-bit totals: visibility queries, throughput
-// queries, rounds (the persistent form: the most tile iterations of any pipeline).
+// ray queue), [4] visibility rows, [5] throughput list length of the current round, [6] round,
+// [7] rays dropped at the per-bounce query cap; then 64-bit totals: visibility queries,
+// throughput queries, rounds (the persistent form: the most tile iterations of any pipeline);
+// then the wavefront form's throughput rows evaluated this round (0 while a short list is
+// carried over) and the rounds the list has been carried over in a row.
 struct Control {
     uint32_t cnt[4];
     uint32_t n_vis, n_thr, round, dropped;
-    unsigned long long tot_vis, tot_thr, tot_rounds, pad;
+    unsigned long long tot_vis, tot_thr, tot_rounds;
+    uint32_t thr_rows, thr_deferred;
 };
 
 __device__ __forceinline__ uint32_t mix32(uint32_t h) {

@@ -13,21 +13,23 @@
 
 namespace nlod {
 
-// Named barrier over the 128 threads of one group (id 1 + group; id 0 is __syncthreads).
+// Named barrier over the N threads of one group (id 1 + group; id 0 is __syncthreads).
+template <uint32_t N = 128>
 __device__ __forceinline__ void group_sync(uint32_t id) {
-    asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory");
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(N) : "memory");
 }
 
-// Group barrier that also ORs a predicate over the group's threads.
+// Group barrier that also ORs a predicate over the group's N threads.
+template <uint32_t N = 128>
 __device__ __forceinline__ bool group_sync_or(uint32_t id, bool v) {
     uint32_t r;
     asm volatile(
         "{\n\t.reg .pred p, q;\n\t"
         "setp.ne.u32 p, %1, 0;\n\t"
-        "bar.red.or.pred q, %2, 128, p;\n\t"
+        "bar.red.or.pred q, %2, %3, p;\n\t"
         "selp.u32 %0, 1, 0, q;\n\t}"
         : "=r"(r)
-        : "r"((uint32_t)v), "r"(id)
+        : "r"((uint32_t)v), "r"(id), "n"(N)
         : "memory");
     return r != 0;
 }

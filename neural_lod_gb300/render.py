@@ -7,8 +7,10 @@
 A frame is one CUDA-graph launch with no host round trip per wavefront (unlike the reference's
 voxel_tracing loop in rptr/cuda/neural-lod/wavefront_neural_throughput_visibility_lod.cu:470-720),
 in one of two forms that give the same pixels: one persistent kernel whose tile pipelines refill
-their ray slots from a queue (tensor-core modules; the default), or rounds in a conditional
-while node in which every ray advances one query (MODE_WAVEFRONT, and the FP32 modules).
+their ray slots from a queue, or rounds in a conditional while node in which every ray advances
+one query (MODE_WAVEFRONT, and the FP32 modules).  MODE_AUTO times both on the scene at creation
+and keeps the faster.  MODE_HOST_ROUNDS issues the wavefront rounds from the host, as the reference
+does (same pixels; every launch visible to a profiler).
 """
 from __future__ import annotations
 
@@ -24,7 +26,7 @@ class _Params(C.Structure):
                 ("up", C.c_float * 3), ("fov_y_deg", C.c_float), ("background", C.c_float * 3), ("env_color", C.c_float * 3),
                 ("lod_max_level", C.c_float), ("lod_input", C.c_float), ("seed", C.c_uint64), ("mode", C.c_uint32)]
 
-MODE_AUTO, MODE_WAVEFRONT, MODE_PERSISTENT = 0, 1, 2     # NLOD_RENDER_*
+MODE_AUTO, MODE_WAVEFRONT, MODE_PERSISTENT, MODE_HOST_ROUNDS = 0, 1, 2, 3     # NLOD_RENDER_*
 
 
 def persistent_form(f: int) -> int:
@@ -101,7 +103,8 @@ class Renderer:
 
     @property
     def mode(self) -> int:
-        """MODE_WAVEFRONT (rounds) or persistent_form(f) (one persistent kernel per frame)."""
+        """MODE_WAVEFRONT (rounds), MODE_HOST_ROUNDS, or persistent_form(f) (one persistent kernel
+        per frame)."""
         return int(self._lib.nlod_renderer_mode(self._r))
 
     @property

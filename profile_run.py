@@ -1,6 +1,7 @@
 """Small, self-contained runs of single kernels of the hot path, for ncu captures.
 
-    python profile_run.py query  [--precision fp16] [--n 2097152] [--iters 3]
+    python profile_run.py query  [--precision fp16] [--n 2097152] [--iters 3] [--variant v]
+    python profile_run.py visq   [--n 65536] [--ml 0.5] [--variant v]
     python profile_run.py train  [--precision fp16] [--n 262144]  [--iters 3]
     python profile_run.py render [--precision fp16] [--iters 3] [--mode 0|1|2] [--size 1024]
     python profile_run.py voxelize [--iters 3]
@@ -56,6 +57,8 @@ def main():
     ap.add_argument("--variant", type=int, default=-1, help="tensor-core kernel variant (-1: autotune)")
     ap.add_argument("--mode", type=int, default=0, help="render form: 0 auto, 1 wavefront, 2 persistent, 256+f one persistent organisation")
     ap.add_argument("--size", type=int, default=1024, help="render image width and height")
+    ap.add_argument("--trace", action="store_true", help="render: per-kernel times from a CUDA activity trace")
+    ap.add_argument("--ml", type=float, default=-1.0, help="visq: one max level fraction for the batch (default: per element)")
     a = ap.parse_args()
 
     import numpy as np
@@ -82,8 +85,10 @@ def main():
         m = N.NetworkWithInputEncoding(6, 1, enc, net, precision=a.precision)
         xv, _, frac = W.visibility_inputs(n, seed=2)
         x = torch.from_numpy(xv).to(dev)
-        f = torch.from_numpy(frac).to(dev)
-        m.set_max_level_gpu(f)
+        if a.ml >= 0:
+            m.set_max_level(a.ml)   # one max level for the batch (the renderer's queries)
+        else:
+            m.set_max_level_gpu(torch.from_numpy(frac).to(dev))
         out = torch.empty((n, 1), device=dev)
         pick_variant(N, m, x, out, a, dev)
         for _ in range(a.iters):
@@ -101,7 +106,24 @@ def main():
         rv.set_params(W.xavier_params(N.layout(venc, vnet, 6, 1), seed=12))
         rt.set_params(W.xavier_params(N.layout(henc, hnet, 10, 3), seed=13))
         p = RenderParams(width=a.size, height=a.size, level=3, lod_max_level=4 / 8, lod_input=3.5 / 8, seed=42, mode=a.mode)
+        if a.precision != "fp32":
+            # the bench's kernel organisations for the frame's rounds
+            rv.set_max_level(p.lod_max_level)
+            rv.autotune(torch.from_numpy(W.visibility_inputs(1 << 20, seed=6)[0]).to(dev), torch.empty((1 << 20, 1), device=dev))
+            rt.autotune(torch.from_numpy(W.throughput_inputs(1 << 16, seed=6)).to(dev), torch.empty((1 << 16, 3), device=dev))
+            print("variants", rv.kernel_variant, rt.kernel_variant)
         r = Renderer(rv, rt, pyr, p)
+        if a.trace:
+            # per-kernel device time of the frames' graph launches, from the CUDA activity trace
+            from torch.profiler import ProfilerActivity, profile
+
+            r.frame()
+            torch.cuda.synchronize()
+            with profile(activities=[ProfilerActivity.CUDA]) as prof:
+                for _ in range(a.iters):
+                    r.frame()
+                torch.cuda.synchronize()
+            print(prof.key_averages().table(sort_by="cuda_time_total", row_limit=25, max_name_column_width=60))
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * a.iters)]
         for i in range(a.iters):
             ev[2 * i].record()

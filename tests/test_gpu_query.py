@@ -165,6 +165,34 @@ def test_every_kernel_variant_and_autotune(cuda, nlod_lib, precision):
     assert 0 <= best < m.n_kernel_variants
 
 
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+def test_every_kernel_variant_visibility_with_lod_mask(cuda, nlod_lib, precision):
+    """The same on the visibility network with a per-element max level: organisations that split a
+    tile row's grid levels between two threads (the LoD mask then falls on either part) compute
+    the same bits as the others."""
+    import torch
+
+    m, orc, params = _net(W.visibility_configs(), 6, 1, precision, grid_scale=0.3)
+    x, _, frac = W.visibility_inputs(4096 + 128 * 3, seed=7)
+    ref = orc.forward(x, params, max_level=frac)
+    m.set_max_level_gpu(torch.from_numpy(frac).to(cuda))
+    xd = torch.from_numpy(x).to(cuda)
+    outs = []
+    for v in range(m.n_kernel_variants):
+        try:
+            m.kernel_variant = v
+        except NlodError as e:
+            assert e.code == 4
+            continue
+        out = m.inference(xd).cpu().numpy()
+        m.sync_status()
+        _check(out, ref, precision)
+        outs.append(out)
+    assert len(outs) >= 10
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+
+
 def test_batch_must_be_multiple_of_128(cuda, nlod_lib):
     import torch
 

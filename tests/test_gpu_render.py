@@ -16,7 +16,7 @@ import oracle
 from neural_lod_gb300 import NetworkWithInputEncoding, workloads as W
 from neural_lod_gb300.lod import LodGrid
 from neural_lod_gb300 import NlodError
-from neural_lod_gb300.render import MODE_PERSISTENT, MODE_WAVEFRONT, RenderParams, Renderer, camera, persistent_form
+from neural_lod_gb300.render import MODE_HOST_ROUNDS, MODE_PERSISTENT, MODE_WAVEFRONT, RenderParams, Renderer, camera, persistent_form
 
 pytestmark = pytest.mark.gpu
 
@@ -127,6 +127,21 @@ def test_persistent_form_matches_wavefront_form(cuda, nlod_lib, precision, shape
     assert np.array_equal(img_p.view(np.uint32), img_w.view(np.uint32))
     assert tot_p[0] == tot_w[0] and tot_p[1] == tot_w[1] and tot_p[3] == tot_w[3]
     assert tot_p[1] > 0
+
+
+@pytest.mark.parametrize("precision", ["fp16", "fp32"])
+def test_host_rounds_match_graph_rounds(cuda, nlod_lib, precision):
+    """The wavefront rounds issued from the host (one list-size read per round) against the same
+    rounds in the frame graph's conditional loop: same pixels, per-ray query counts and totals,
+    rounds included; a query cap that drops rays included."""
+    bits, res, levels = _scene()
+    grid = LodGrid(bits, res, levels)
+    params = RenderParams(width=96, height=64, level=1, max_depth=4, max_vis_queries=24, lod_max_level=6 / 8, lod_input=1.5 / 8)
+    img_h, st_h, tot_h = _frame(precision, params, grid, MODE_HOST_ROUNDS)
+    img_g, st_g, tot_g = _frame(precision, params, grid, MODE_WAVEFRONT)
+    assert np.array_equal(st_h, st_g)
+    assert np.array_equal(img_h.view(np.uint32), img_g.view(np.uint32))
+    assert tot_h == tot_g and tot_h[2] >= 2
 
 
 def test_persistent_form_needs_tensor_core_modules(cuda, nlod_lib):
