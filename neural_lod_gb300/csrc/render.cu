@@ -146,7 +146,11 @@ __global__ void __launch_bounds__(256) k_step(const __grid_constant__ RenderCons
 }
 
 // Publishes the lists built this round, resets the other parity, sets the loop condition.
-__global__ void k_round(Control* ctl, uint32_t max_rounds, uint32_t* status, cudaGraphConditionalHandle cond, int use_cond) {
+// use_cond: the launch is the loop body's (graph form): it sets the loop condition and the
+// condition of the next round's throughput inference (skipped in rounds that carry the list over
+// or have none).
+__global__ void k_round(Control* ctl, uint32_t max_rounds, uint32_t* status, cudaGraphConditionalHandle cond,
+                        cudaGraphConditionalHandle thr_cond, int use_cond) {
     const uint32_t q = ctl->round & 1u;
     const uint32_t nv = ctl->cnt[q * 2 + 0], nt = ctl->cnt[q * 2 + 1];
     // A short throughput list waits for more rows instead of paying a whole inference launch for a
@@ -170,12 +174,53 @@ __global__ void k_round(Control* ctl, uint32_t max_rounds, uint32_t* status, cud
         atomicOr(status, 4u);
         more = false;
     }
-    if (use_cond) cudaGraphSetConditional(cond, more ? 1u : 0u);
+    if (use_cond) {
+        cudaGraphSetConditional(cond, more ? 1u : 0u);
+        cudaGraphSetConditional(thr_cond, ctl->thr_rows > 0u ? 1u : 0u);
+    }
 }
 
 __global__ void k_reset(Control* ctl) {
     Control c{};
     *ctl = c;
+}
+
+// Appends to the graph being captured on `s` a conditional node of `type` (its condition set by
+// kernels of that graph; no value is assigned at launch) whose body is what `body(stream)`
+// records, and makes it the capture's next dependency.
+template <typename Body>
+cudaError_t add_conditional_body(cudaStream_t s, cudaGraphConditionalNodeType type, cudaGraphConditionalHandle* handle, Body&& body) {
+    cudaStreamCaptureStatus cst;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t n_deps = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &cst, nullptr, &g, &deps, nullptr, &n_deps);
+    if (e != cudaSuccess) return e;
+    e = cudaGraphConditionalHandleCreate(handle, g, 0, 0);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = *handle;
+    cp.conditional.type = type;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, n_deps, &cp);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return e;
+    cudaGraph_t inner = cp.conditional.phGraph_out[0];
+    cudaStream_t bs;
+    e = cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamBeginCaptureToGraph(bs, inner, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        e = body(bs);
+        cudaGraph_t out = inner;
+        const cudaError_t e2 = cudaStreamEndCapture(bs, &out);
+        if (e == cudaSuccess) e = e2;
+    }
+    cudaStreamDestroy(bs);
+    return e;
 }
 
 }  // namespace
@@ -446,7 +491,7 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
             k_reset<<<1, 1, 0, s>>>(B.ctl);
             k_step<<<blocks, 256, 0, s>>>(C, B, 1);
-            k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, B.status, 0, 0);
+            k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, B.status, 0, 0, 0);
             cudaStreamCaptureStatus cst;
             cudaGraph_t cap_graph = nullptr;
             const cudaGraphNode_t* deps = nullptr;
@@ -468,10 +513,15 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             cudaError_t e = cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
                 e = module_inference_device_count(r->vis, r->n_pad, B.vis_in, B.vis_out, &B.ctl->n_vis, r->vis_max_level, bs);
-                if (e == cudaSuccess) e = module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, bs);
+                // the throughput inference inside an if node: most rounds carry its list over (or
+                // have none), and a launch that finds no rows still costs its grid's start-up
+                cudaGraphConditionalHandle thr_cond{};
+                if (e == cudaSuccess) e = add_conditional_body(bs, cudaGraphCondTypeIf, &thr_cond, [&](cudaStream_t ts) {
+                    return module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, ts);
+                });
                 if (e == cudaSuccess) {
                     k_step<<<blocks, 256, 0, bs>>>(C, B, 0);
-                    k_round<<<1, 1, 0, bs>>>(B.ctl, C.max_rounds, B.status, cond, 1);
+                    k_round<<<1, 1, 0, bs>>>(B.ctl, C.max_rounds, B.status, cond, thr_cond, 1);
                     e = cudaGetLastError();
                 }
                 cudaGraph_t body_out = body;
@@ -503,7 +553,7 @@ int nlod_render_frame(nlod_renderer* r, void* stream, float* image, uint32_t* ra
             const RenderConsts& C = r->C;
             k_reset<<<1, 1, 0, s>>>(B.ctl);
             k_step<<<r->step_blocks, 256, 0, s>>>(C, B, 1);
-            k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, B.status, 0, 0);
+            k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, B.status, 0, 0, 0);
             cuda_check(cudaGetLastError(), "launch");
             for (;;) {
                 Control c;
@@ -513,7 +563,7 @@ int nlod_render_frame(nlod_renderer* r, void* stream, float* image, uint32_t* ra
                 cuda_check(module_inference_device_count(r->vis, r->n_pad, B.vis_in, B.vis_out, &B.ctl->n_vis, r->vis_max_level, s), "inference");
                 cuda_check(module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, s), "inference");
                 k_step<<<r->step_blocks, 256, 0, s>>>(C, B, 0);
-                k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, B.status, 0, 0);
+                k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, B.status, 0, 0, 0);
                 cuda_check(cudaGetLastError(), "launch");
             }
         } else {
