@@ -88,13 +88,25 @@ __device__ __forceinline__ void hdda_update(Hdda& h, const float (&E)[3], const 
     }
 }
 
+// One step along the axis with the nearest crossing.  The axis is applied through selects rather
+// than an index, so that the state stays in registers (an indexed array lives in local memory).
 __device__ __forceinline__ bool hdda_step(Hdda& h) {
-    const int a = (h.next[0] < h.next[1] && h.next[0] < h.next[2]) ? 0 : (h.next[1] < h.next[2] ? 1 : 2);
-    float na = h.next[a];
+    const bool x = h.next[0] < h.next[1] && h.next[0] < h.next[2];
+    const bool y = !x && h.next[1] < h.next[2];
+    const bool z = !x && !y;
+    float na = x ? h.next[0] : (y ? h.next[1] : h.next[2]);
     if (na <= h.t0) na = __fadd_rn(na, __fadd_rn(__fsub_rn(h.t0, __fmul_rn(0.999999f, na)), 1.0e-6f));
     h.t0 = na;
-    h.next[a] = __fadd_rn(na, __fmul_rn((float)h.dim, h.delta[a]));
-    h.voxel[a] += h.dim * h.step[a];
+    const float delta = x ? h.delta[0] : (y ? h.delta[1] : h.delta[2]);
+    const int32_t step = x ? h.step[0] : (y ? h.step[1] : h.step[2]);
+    const float nn = __fadd_rn(na, __fmul_rn((float)h.dim, delta));
+    const int32_t dv = h.dim * step;
+    h.next[0] = x ? nn : h.next[0];
+    h.next[1] = y ? nn : h.next[1];
+    h.next[2] = z ? nn : h.next[2];
+    h.voxel[0] += x ? dv : 0;
+    h.voxel[1] += y ? dv : 0;
+    h.voxel[2] += z ? dv : 0;
     return h.t0 <= h.t1;
 }
 

@@ -81,7 +81,8 @@ constexpr uint32_t kThrDeferBelow = 32768u;
 constexpr uint32_t kThrDeferRounds = 8u;
 
 // One round for every queued ray (first = true: ray generation, every pixel's ray).
-__global__ void __launch_bounds__(256) k_step(const __grid_constant__ RenderConsts C, RenderBufs B, int first) {
+// Four 256-thread blocks per SM: 64 registers, which the DDA's state fits without spilling.
+__global__ void __launch_bounds__(256, 4) k_step(const __grid_constant__ RenderConsts C, RenderBufs B, int first) {
     const uint32_t round = first ? 0u : B.ctl->round;
     const uint32_t p = (round + 1u) & 1u, q = round & 1u;   // lists read / written
     const uint32_t nv = first ? C.n_rays : B.ctl->n_vis;
