@@ -3,7 +3,7 @@
     python profile_run.py query  [--precision fp16] [--n 2097152] [--iters 3] [--variant v]
     python profile_run.py visq   [--n 65536] [--ml 0.5] [--variant v]
     python profile_run.py train  [--precision fp16] [--n 262144]  [--iters 3]
-    python profile_run.py render [--precision fp16] [--iters 3] [--mode 0|1|2] [--size 1024]
+    python profile_run.py render [--precision fp16] [--iters 3] [--mode 0|1|2|3|256+f] [--size 1024]
     python profile_run.py voxelize [--iters 3]
     python profile_run.py sampler  [--iters 3]
 
@@ -55,9 +55,9 @@ def main():
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--iters", type=int, default=3)
     ap.add_argument("--variant", type=int, default=-1, help="tensor-core kernel variant (-1: autotune)")
-    ap.add_argument("--mode", type=int, default=0, help="render form: 0 auto, 1 wavefront, 2 persistent, 256+f one persistent organisation")
+    ap.add_argument("--mode", type=int, default=0,
+                    help="render form: 0 auto, 1 wavefront, 2 persistent, 3 host-issued rounds, 256+f one persistent organisation")
     ap.add_argument("--size", type=int, default=1024, help="render image width and height")
-    ap.add_argument("--trace", action="store_true", help="render: per-kernel times from a CUDA activity trace")
     ap.add_argument("--ml", type=float, default=-1.0, help="visq: one max level fraction for the batch (default: per element)")
     a = ap.parse_args()
 
@@ -113,17 +113,6 @@ def main():
             rt.autotune(torch.from_numpy(W.throughput_inputs(1 << 16, seed=6)).to(dev), torch.empty((1 << 16, 3), device=dev))
             print("variants", rv.kernel_variant, rt.kernel_variant)
         r = Renderer(rv, rt, pyr, p)
-        if a.trace:
-            # per-kernel device time of the frames' graph launches, from the CUDA activity trace
-            from torch.profiler import ProfilerActivity, profile
-
-            r.frame()
-            torch.cuda.synchronize()
-            with profile(activities=[ProfilerActivity.CUDA]) as prof:
-                for _ in range(a.iters):
-                    r.frame()
-                torch.cuda.synchronize()
-            print(prof.key_averages().table(sort_by="cuda_time_total", row_limit=25, max_name_column_width=60))
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * a.iters)]
         for i in range(a.iters):
             ev[2 * i].record()
