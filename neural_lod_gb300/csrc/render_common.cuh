@@ -130,6 +130,14 @@ enum : int { MARCH_DONE = 0, MARCH_VIS = 1, MARCH_FAIL = 2, MARCH_DROPPED = 3 };
 // (voxel, t_near / t_far, query count).  MARCH_DONE: the ray escaped and its pixel is written
 // (background before the first bounce, environment times throughput after).  MARCH_DROPPED: the
 // per-bounce query cap was reached.  MARCH_FAIL: the DDA ran out of its step budget.
+// The pixel of a ray that escaped: the background before the first bounce, the environment
+// times the path throughput after.
+__device__ __forceinline__ void write_escape(const RenderConsts& C, const RayState& st, float* __restrict__ pixel) {
+    const uint32_t bounce = st.meta & 0xFFu;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) pixel[k] = bounce == 0 ? C.background[k] : __fmul_rn(st.tp[k], C.env[k]);
+}
+
 __device__ __forceinline__ int ray_march(const RenderConsts& C, RayState& st, float* __restrict__ pixel) {
     const uint32_t nvis = (st.meta >> 8) & 0xFFFFu;
     if (nvis >= C.max_vis) return MARCH_DROPPED;
@@ -138,9 +146,7 @@ __device__ __forceinline__ int ray_march(const RenderConsts& C, RayState& st, fl
     const int r = dda::first_active_voxel(C.L, st.o, st.d, st.tmin, st.ijk, v3, tn, tf, C.budget);
     if (r < 0) return MARCH_FAIL;
     if (r == 0) {
-        const uint32_t bounce = st.meta & 0xFFu;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) pixel[k] = bounce == 0 ? C.background[k] : __fmul_rn(st.tp[k], C.env[k]);
+        write_escape(C, st, pixel);
         return MARCH_DONE;
     }
 #pragma unroll
