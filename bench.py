@@ -55,7 +55,8 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms while the timed region runs."""
+    """nvidia-smi clocks/throttle reasons sampled every 20 ms while the timed region runs; entering
+    waits (up to 3 s) for the first sample, so that the samples cover the region."""
 
     FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
@@ -69,9 +70,18 @@ class ClockSampler:
         try:
             self.fh = open(self.out_path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-lms", "200", "-i", str(self.dev)], stdout=self.fh, stderr=subprocess.DEVNULL)
+                                          "-lms", "20", "-i", str(self.dev)], stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return self
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+            try:
+                if self.out_path.stat().st_size > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.01)
         return self
 
     def __exit__(self, *a):

@@ -20,7 +20,12 @@ Bounds (relative L2 error per block), from the measurements printed by this test
   after 30 steps (BCE 0.14; many outputs reach the loss's clamp at 1e-5 / 1 - 1e-5, where the
   loss is not differentiable, so central differences no longer pin the gradient and the FP16
   forward's rounding is felt by the nearly fitted samples)
-      FP32 1e-4 (measured <= 1e-6), FP16 3e-2 (measured <= 1.4e-2), BF16 8e-2 (measured <= 4.1e-2).
+      FP32: 1,024 sampled parameters 1e-4 (measured <= 8e-7), the network weights 1e-3 and the
+      grid tables 5e-3 (measured 1e-6 .. 8.1e-5 and 1e-6 .. 1.2e-3 over runs: the trained point
+      varies from run to run with the order of the training step's atomic sums, and a sample
+      whose output lands within single-precision rounding of the clamp or of a ReLU kink takes
+      a different derivative in FP32 and FP64, which shows in the few entries it touches);
+      FP16 3e-2 (measured <= 1.4e-2), BF16 8e-2 (measured <= 4.1e-2).
 The grid-table gradients of the FP16 form are sums over the few samples that touch each entry,
 evaluated with FP16 tables, FP16 encoded features and FP16 activations (tiny-cuda-nn's own
 precision); the network weights' gradients sum over every sample and meet 1e-3.
@@ -36,7 +41,7 @@ pytestmark = pytest.mark.gpu
 N = 1 << 18
 # (steps) -> precision -> (network-weight blocks, grid block, 1,024 sampled parameters)
 BOUNDS = {10: {"fp32": (1e-4, 1e-4, 1e-4), "fp16": (1e-3, 1e-2, 1e-3), "bf16": (3e-2, 3e-2, 3e-2)},
-          30: {"fp32": (1e-4, 1e-4, 1e-4), "fp16": (3e-2, 3e-2, 3e-2), "bf16": (8e-2, 8e-2, 8e-2)}}
+          30: {"fp32": (1e-3, 5e-3, 1e-4), "fp16": (3e-2, 3e-2, 3e-2), "bf16": (8e-2, 8e-2, 8e-2)}}
 
 
 def _rel(a, b):
