@@ -228,6 +228,19 @@ NLOD_API int nlod_get_kernel_variant(const nlod_module* m);
 NLOD_API int nlod_set_kernel_variant(nlod_module* m, int variant);
 NLOD_API int nlod_autotune(nlod_module* m, void* stream, uint32_t n, const float* in, float* out);
 
+/*
+ * Calibration (diagnostics; no tiny-cuda-nn counterpart): the memory-side floors of the hot path
+ * on this module's grid, each kernel alone at full occupancy, timed with CUDA events on `stream`
+ * (synchronous).  nlod_calib_gathers: the encoding's grid gathers of n queries (from the FP16
+ * table copy when the module keeps one) -- the floor of the query kernel and of the training
+ * encoding.  nlod_calib_scatter: the grid-gradient scatter of n samples (one reduction per corner,
+ * x-adjacent aligned pairs merged) -- the floor of the fused training kernel; it overwrites the
+ * module's gradient buffer (the next training step clears it).  Positions are seeded U[0,1)^3.
+ * ms_out receives the kernel's duration.
+ */
+NLOD_API int nlod_calib_gathers(nlod_module* m, void* stream, uint32_t n, float* ms_out);
+NLOD_API int nlod_calib_scatter(nlod_module* m, void* stream, uint32_t n, float* ms_out);
+
 /* ---- LoD occupancy pyramid and first-active-voxel search ----------------------------------
  * The reference builds one NanoVDB grid per LoD from the voxelizer's point cloud, level k holding
  * voxel (x,y,z) >> k (rptr/cuda/neural-lod/neural_lod_learning_init.cu:194-267), and marches

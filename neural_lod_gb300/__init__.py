@@ -195,6 +195,20 @@ class NetworkWithInputEncoding:
         check(self._lib.nlod_autotune(self._m, _stream_ptr(stream), x.shape[0], _ptr(x), _ptr(out)))
         return self.kernel_variant
 
+    def calib_gathers(self, n: int, stream=None) -> float:
+        """Duration (ms) of the encoding's grid gathers alone for n seeded queries
+        (nlod_calib_gathers): the memory-side floor of the query kernel."""
+        ms = C.c_float()
+        check(self._lib.nlod_calib_gathers(self._m, _stream_ptr(stream), n, C.byref(ms)))
+        return ms.value
+
+    def calib_scatter(self, n: int, stream=None) -> float:
+        """Duration (ms) of the grid-gradient scatter alone for n seeded samples
+        (nlod_calib_scatter; overwrites the gradient buffer): the floor of the fused training kernel."""
+        ms = C.c_float()
+        check(self._lib.nlod_calib_scatter(self._m, _stream_ptr(stream), n, C.byref(ms)))
+        return ms.value
+
     def sync_status(self, stream=None) -> None:
         """Synchronises `stream` and raises NlodError if a kernel reported a device-side error
         (for example a wait that gave up) since the last check."""

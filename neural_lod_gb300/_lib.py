@@ -62,6 +62,8 @@ SIGNATURES = [
     ("nlod_get_kernel_variant", C.c_int, [_vp]),
     ("nlod_set_kernel_variant", C.c_int, [_vp, C.c_int]),
     ("nlod_autotune", C.c_int, [_vp, _vp, _u32, _fp, _fp]),
+    ("nlod_calib_gathers", C.c_int, [_vp, _vp, _u32, C.POINTER(C.c_float)]),
+    ("nlod_calib_scatter", C.c_int, [_vp, _vp, _u32, C.POINTER(C.c_float)]),
     ("nlod_sync_status", C.c_int, [_vp, _vp]),
     ("nlod_lod_grid_create", C.c_int, [_fp, _u32, _u32, _vp, C.POINTER(_vp)]),
     ("nlod_lod_grid_destroy", None, [_vp]),

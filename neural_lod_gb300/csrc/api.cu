@@ -306,6 +306,30 @@ bool module_tc_operands(nlod_module* m, const ModelDesc** d, const void** weight
 
 }  // namespace nlod
 
+namespace {
+
+// Times `launch` on stream s with CUDA events (synchronous); ms = its duration.
+template <typename Launch>
+void time_on_stream(cudaStream_t s, float* ms, Launch&& launch) {
+    cudaEvent_t e0, e1;
+    cuda_check(cudaEventCreate(&e0), "event");
+    cudaError_t e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cuda_check(e, "event");
+    }
+    e = cudaEventRecord(e0, s);
+    if (e == cudaSuccess) e = launch();
+    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cuda_check(e, "calibration");
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* nlod_last_error(void) { return g_last_error.c_str(); }
@@ -1050,6 +1074,28 @@ int nlod_autotune(nlod_module* m, void* stream, uint32_t n, const float* in, flo
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         m->tc_variant = best_v;
+    });
+}
+
+int nlod_calib_gathers(nlod_module* m, void* stream, uint32_t n, float* ms_out) {
+    return guarded([&] {
+        if (!m || !ms_out) throw Error(NLOD_ERR_INVALID, "module and ms_out must not be NULL");
+        if (m->d.n_grids == 0) throw Error(NLOD_ERR_UNSUPPORTED, "the module has no grid encoding");
+        cudaStream_t s = (cudaStream_t)stream;
+        // the gathers' results go into a sum that is stored (to the gradient buffer's first entry,
+        // which the next training step clears) only if it equals a value no table sum takes
+        const bool half = m->grid_h != nullptr;
+        const void* tables = half ? static_cast<const void*>(m->grid_h) : static_cast<const void*>(m->inference_params());
+        time_on_stream(s, ms_out, [&] { return launch_calib_gathers(m->d, tables, half, n, m->grads, s); });
+    });
+}
+
+int nlod_calib_scatter(nlod_module* m, void* stream, uint32_t n, float* ms_out) {
+    return guarded([&] {
+        if (!m || !ms_out) throw Error(NLOD_ERR_INVALID, "module and ms_out must not be NULL");
+        if (m->d.n_grids == 0) throw Error(NLOD_ERR_UNSUPPORTED, "the module has no grid encoding");
+        cudaStream_t s = (cudaStream_t)stream;
+        time_on_stream(s, ms_out, [&] { return launch_calib_scatter(m->d, m->grads, n, s); });
     });
 }
 

@@ -1,0 +1,117 @@
+// Calibration kernels: the two memory-side floors of the hot path, measured on a module's own
+// grid with nothing else in the kernel.
+//   k_calib_gathers     the encoding's grid gathers of n queries (grid_group_forward of every grid
+//                       slot, from the FP16 copy of the tables when the module keeps one) at full
+//                       occupancy: the floor of the query kernel and of the training encoding.
+//   k_calib_scatter     the grid-gradient scatter of n samples (grid_level_scatter8 of every level,
+//                       one FP32x2 or paired FP32x4 reduction per corner), the floor of the fused
+//                       training kernel.
+// Positions are U[0,1)^3 from a hash of the element index, so no input is read.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "desc.h"
+#include "encoding.cuh"
+#include "kernels.h"
+
+namespace nlod {
+namespace {
+
+constexpr int kCalibThreads = 256;
+
+__device__ __forceinline__ uint32_t calib_hash(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+__device__ __forceinline__ float calib_u01(uint32_t i, uint32_t k) { return (float)(calib_hash(3u * i + k) >> 8) * (1.0f / 16777216.0f); }
+
+template <typename TT>
+__global__ void __launch_bounds__(kCalibThreads) k_calib_gathers(const __grid_constant__ ModelDesc d, const TT* __restrict__ params, uint32_t n,
+                                                                 float* __restrict__ sink) {
+    __shared__ GridLevel lvl[kMaxGrids * kMaxLevels];
+    for (uint32_t i = threadIdx.x; i < d.n_grids * (uint32_t)kMaxLevels; i += blockDim.x) {
+        const uint32_t g = i / kMaxLevels, l = i % kMaxLevels;
+        if (l < d.grids[g].n_levels) lvl[i] = d.grids[g].levels[l];
+    }
+    __syncthreads();
+    float acc = 0.f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float px = calib_u01(i, 0), py = calib_u01(i, 1), pz = calib_u01(i, 2);
+        for (uint32_t si = 0; si < d.n_slots; ++si) {
+            const Slot& s = d.slots[si];
+            if (s.type != SLOT_GRID) continue;
+            const GridDesc& g = d.grids[s.grid];
+#pragma unroll 1
+            for (uint32_t l = 0; l < g.n_levels; ++l) {
+                float f[2];
+                grid_group_forward<1, TT>(g, lvl + s.grid * kMaxLevels, l, 1u, params + g.param_offset, px, py, pz, 1000.f, f);
+                acc += f[0] + f[1];
+            }
+        }
+    }
+    if (acc == 1.2345e30f) sink[0] = acc;   // keeps the gathers alive; never true for table values
+}
+
+__global__ void __launch_bounds__(kCalibThreads) k_calib_scatter(const __grid_constant__ ModelDesc d, float* __restrict__ grads, uint32_t n) {
+    __shared__ GridLevel lvl[kMaxGrids * kMaxLevels];
+    for (uint32_t i = threadIdx.x; i < d.n_grids * (uint32_t)kMaxLevels; i += blockDim.x) {
+        const uint32_t g = i / kMaxLevels, l = i % kMaxLevels;
+        if (l < d.grids[g].n_levels) lvl[i] = d.grids[g].levels[l];
+    }
+    __syncthreads();
+    // a grid-stride loop that every lane of a warp runs the same number of times (the scatter
+    // must be called by all lanes)
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n + stride - 1) / stride;
+    for (uint32_t k = 0; k < rounds; ++k) {
+        const uint32_t i = k * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const bool act = i < n;
+        const float px = calib_u01(i, 0), py = calib_u01(i, 1), pz = calib_u01(i, 2);
+        for (uint32_t si = 0; si < d.n_slots; ++si) {
+            const Slot& s = d.slots[si];
+            if (s.type != SLOT_GRID) continue;
+            const GridDesc& g = d.grids[s.grid];
+            uint32_t p0, p1, p2;
+            hash_primes(g.hash, p0, p1, p2);
+#pragma unroll 1
+            for (uint32_t level = 0; level < g.n_levels; ++level)
+                grid_level_scatter8<false>(g, lvl[s.grid * kMaxLevels + level], grads + g.param_offset, p0, p1, p2, px, py, pz,
+                                           make_float2(1e-3f, -1e-3f), act);
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_calib_gathers(const ModelDesc& d, const void* params, bool half_tables, uint32_t n, float* sink, cudaStream_t s) {
+    int sms = 0, dev = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const void* kern = half_tables ? (const void*)k_calib_gathers<__half> : (const void*)k_calib_gathers<float>;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCalibThreads, 0);
+    if (e != cudaSuccess) return e;
+    const uint32_t blocks = (uint32_t)(sms * (per_sm > 0 ? per_sm : 1));
+    if (half_tables) k_calib_gathers<__half><<<blocks, kCalibThreads, 0, s>>>(d, static_cast<const __half*>(params), n, sink);
+    else k_calib_gathers<float><<<blocks, kCalibThreads, 0, s>>>(d, static_cast<const float*>(params), n, sink);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_calib_scatter(const ModelDesc& d, float* grads, uint32_t n, cudaStream_t s) {
+    int sms = 0, dev = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_calib_scatter, kCalibThreads, 0);
+    if (e != cudaSuccess) return e;
+    k_calib_scatter<<<(uint32_t)(sms * (per_sm > 0 ? per_sm : 1)), kCalibThreads, 0, s>>>(d, grads, n);
+    return cudaGetLastError();
+}
+
+}  // namespace nlod

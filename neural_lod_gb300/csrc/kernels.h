@@ -174,6 +174,10 @@ bool tc_variant_ok(const ModelDesc& d, int variant, int kind = 1);
 int tc_default_variant(const ModelDesc& d);
 cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, int variant, uint32_t* status, cudaStream_t s);
 
+// calib.cu
+cudaError_t launch_calib_gathers(const ModelDesc& d, const void* params, bool half_tables, uint32_t n, float* sink, cudaStream_t s);
+cudaError_t launch_calib_scatter(const ModelDesc& d, float* grads, uint32_t n, cudaStream_t s);
+
 // Fused tensor-core training step (train_tc.cu): encoding, forward, loss, backward, weight
 // gradients and grid-gradient scatter.  grads must be zeroed by the caller; gradients are
 // accumulated as dL/dparam * grad_scale.

@@ -6,6 +6,7 @@
     python profile_run.py render [--precision fp16] [--iters 3] [--mode 0|1|2|3|256+f] [--size 1024]
     python profile_run.py voxelize [--iters 3]
     python profile_run.py sampler  [--iters 3]
+    python profile_run.py calib    [--n 2097152] [--iters 5]   # gather / scatter floors
 
 `query` runs the throughput-query forward (the bench's headline kernel) `iters` times on the
 bench's inputs; `train` runs visibility training steps.  Each run ends with a status check, so a
@@ -50,7 +51,7 @@ def pick_variant(N, m, x, out, a, dev):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["query", "train", "train_thr", "visq", "render", "voxelize", "sampler"])
+    ap.add_argument("what", choices=["query", "train", "train_thr", "visq", "render", "voxelize", "sampler", "calib"])
     ap.add_argument("--precision", default="fp16")
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--iters", type=int, default=3)
@@ -140,6 +141,27 @@ def main():
         sp.sync_status()
         torch.cuda.synchronize()
         print("ok sampler")
+        return
+    elif a.what == "calib":
+        # the memory-side floors on the bench's grids: the throughput query's gathers (2^21 queries,
+        # FP16 tables) and the training scatters (throughput 2^20, visibility 2^18 samples)
+        import statistics
+
+        enc, net = W.throughput_configs()
+        m = N.NetworkWithInputEncoding(10, 3, enc, net, loss=W.THROUGHPUT_LOSS, optimizer=W.THROUGHPUT_OPTIMIZER, precision="fp16")
+        m.set_params(W.xavier_params(N.layout(enc, net, 10, 3), seed=10))
+        nq = a.n or W.WORKLOADS["throughput_query"]["batch"]
+        g = [m.calib_gathers(nq) for _ in range(max(3, a.iters))]
+        st = [m.calib_scatter(1 << 20) for _ in range(max(3, a.iters))]
+        venc, vnet = W.visibility_configs(16)
+        mv = N.NetworkWithInputEncoding(6, 1, venc, vnet, loss=W.VISIBILITY_LOSS, optimizer=W.VISIBILITY_OPTIMIZER, precision="fp16")
+        mv.set_params(W.xavier_params(N.layout(venc, vnet, 6, 1), seed=11))
+        sv = [mv.calib_scatter(1 << 18) for _ in range(max(3, a.iters))]
+        print(f"gathers of {nq} throughput queries: median {statistics.median(g):.4f} ms ({[round(v, 4) for v in g]})")
+        print(f"scatter of 2^20 throughput samples: median {statistics.median(st):.4f} ms")
+        print(f"scatter of 2^18 visibility samples: median {statistics.median(sv):.4f} ms")
+        m.sync_status()
+        mv.sync_status()
         return
     elif a.what == "voxelize":
         from neural_lod_gb300 import voxelize as V

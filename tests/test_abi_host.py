@@ -134,6 +134,8 @@ def test_entry_points_reject_null_arguments_before_touching_the_gpu(nlod_lib):
         "nlod_forward": lambda: L.nlod_forward(None, None, 128, None, None, None),
         "nlod_optimizer_step": lambda: L.nlod_optimizer_step(None, None),
         "nlod_autotune": lambda: L.nlod_autotune(None, None, 128, None, None),
+        "nlod_calib_gathers": lambda: L.nlod_calib_gathers(None, None, 128, None),
+        "nlod_calib_scatter": lambda: L.nlod_calib_scatter(None, None, 128, None),
         "nlod_serialize": lambda: L.nlod_serialize(None, 1, C.byref(out)),
         "nlod_deserialize": lambda: L.nlod_deserialize(None, b"{}"),
         "nlod_set_params": lambda: L.nlod_set_params(None, None, 0, 0),

@@ -258,3 +258,36 @@ def test_inference_after_training_reads_current_grid_tables(cuda, nlod_lib, with
     fresh = NetworkWithInputEncoding(10, 3, enc, net, precision="fp16")
     fresh.set_params(m.get_params("inference"))
     assert torch.equal(fresh.inference(x), y1)
+
+
+def test_calibration_floors(cuda, nlod_lib):
+    """The gather and scatter floors run on a module's grid and take less time than the kernels
+    they bound: the query kernel does the same gathers and more, the training step the same
+    scatter and more."""
+    import torch
+
+    enc, net = W.throughput_configs()
+    m = NetworkWithInputEncoding(10, 3, enc, net, loss=W.THROUGHPUT_LOSS, optimizer=W.THROUGHPUT_OPTIMIZER, precision="fp16")
+    m.set_params(W.xavier_params(oracle.model_spec(enc, net, 10, 3), seed=10))
+    n = 1 << 17
+    x = torch.from_numpy(W.throughput_inputs(n, seed=1)).to(cuda)
+    out = torch.empty((n, 3), device=cuda)
+    for _ in range(2):
+        g = m.calib_gathers(n)
+        s = m.calib_scatter(n)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    m.inference(x, out)
+    e0.record()
+    m.inference(x, out)
+    e1.record()
+    e1.synchronize()
+    q = e0.elapsed_time(e1)
+    m.sync_status()
+    print(f"\ngathers {g:.4f} ms, scatter {s:.4f} ms, query {q:.4f} ms for {n} elements")
+    assert 0.0 < g < 1.5 * q
+    assert s > 0.0
+    # the scatter left the gradients dirty: a training step starts from cleared gradients
+    t = torch.rand((n, 3), device=cuda)
+    loss = m.training_step(x, t).item()
+    m.sync_status()
+    assert np.isfinite(loss)
