@@ -307,8 +307,9 @@ NLOD_API int nlod_voxelize(const float* triangles, uint64_t n_triangles, uint32_
  * check_visibility, process_ray_bounce) without the host round trip per wavefront.  A frame is one
  * CUDA-graph launch, in one of two forms: the persistent form (tensor-core modules) is one kernel
  * whose tile pipelines refill their ray slots from a queue and run both networks on full tiles;
- * the wavefront form advances every ray one query per round, the rounds running in a conditional
- * while node.  Both forms give the same pixels and query counts.
+ * the wavefront form advances every ray by rounds (one round: a chain of visibility queries marched
+ * ahead, or a throughput query), the rounds running in a conditional while node.  Both forms give
+ * the same pixels and query counts.
  * Network inputs: visibility = (voxel-local entry point in [0,1]^3, (dir + 1) / 2) with
  * lod_max_level as the grid's max level; throughput = (voxel centre / res, (wi + 1) / 2,
  * (wo + 1) / 2, lod_input), wo = -dir.  Camera and radiance parameters are the renderer's. */
@@ -332,6 +333,13 @@ typedef struct nlod_render_params {
                                       creation; else the wavefront rounds.
                                       NLOD_RENDER_WAVEFRONT / NLOD_RENDER_PERSISTENT force one form;
                                       NLOD_RENDER_HOST_ROUNDS issues the wavefront rounds from the host */
+    uint32_t max_chain;            /* wavefront forms: most visibility queries a ray marches ahead in one
+                                      round (query k+1 is the march that follows query k's rejection; the
+                                      queries past an accepted one are dropped, so pixels and counts do not
+                                      depend on it).  Each round's chain length is the longest power of two
+                                      up to this cap whose expected dropped queries stay near 3 %, from the
+                                      last round's accepted fraction.  0: 8; at most 64; the cap also keeps
+                                      the visibility rows within 2^23 (one query per round beyond that) */
 } nlod_render_params;
 
 #define NLOD_RENDER_AUTO 0

@@ -11,15 +11,18 @@
 //   throughput input  = voxel centre / res, (wi + 1) / 2, (wo + 1) / 2, LoD column.
 //
 // GB300 organisation.  The reference synchronises with the host after every wavefront to size
-// the next launch.  Here every ray advances independently by one query per round, and one round
-// is four launches: visibility inference and throughput inference over the current lists (the
-// tensor-core kernels read their row count from device memory), k_step (resolve every queued
-// ray: accept / reject the voxel, apply a throughput result and bounce, march to the next
-// occupied voxel with the bit-exact DDA, append the ray's next query to the compacted lists with
-// warp-aggregated atomics) and k_round (publish the list sizes, set the loop condition).  The
-// rounds run inside a CUDA graph as the body of a conditional while node, so a frame is one
-// graph launch with no host round trip; the loop ends when both lists are empty (bounded by
-// construction: each round moves every live ray one query forward).
+// the next launch.  Here every ray advances independently, and one round is four launches:
+// visibility inference and throughput inference over the current lists (the tensor-core kernels
+// read their row count from device memory), k_step (resolve every queued ray: apply its chain of
+// visibility values up to the first accepted one, apply a throughput result and bounce, march the
+// next chain of occupied voxels with the bit-exact DDA, append the ray and its query rows to the
+// compacted lists with warp-aggregated atomics) and k_round (publish the list sizes, set the next
+// chain length and the loop condition).  The rounds run inside a CUDA graph as the body of a
+// conditional while node, so a frame is one graph launch with no host round trip; the loop ends
+// when both lists are empty (bounded by construction: each round moves every live ray at least
+// one query forward).  A chain of visibility queries marched ahead (k_step) takes a ray through
+// several rejected voxels per round, so a frame whose voxels are mostly rejected needs a few
+// rounds instead of one per voxel.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -54,13 +57,16 @@ struct RenderBufs {
     RayState* rays;
     uint32_t* lists;      // [2 parity][2 kind][n_rays]
     Control* ctl;
-    float* vis_in;        // [n_pad][6]
-    float* vis_out;       // [n_pad][1]
+    float* vis_in;        // [max_chain * n_pad][6]
+    float* vis_out;       // [max_chain * n_pad][1]
     float* thr_in;        // [n_pad][10]
     float* thr_out;       // [n_pad][3]
     float* image;         // [n_rays][3]
     uint32_t* ray_stats;  // [n_rays][2]
     uint32_t* status;
+    int4* chain_q;        // [max_chain][n_rays] a chain's queries: voxel, t_near bits
+    float* chain_t;       // [max_chain][n_rays] their t_far
+    uint32_t* vis_row0;   // [2 parity][n_rays] first visibility row of each visibility-list entry
 };
 
 // Appends the lanes with `want` to a list; returns each wanting lane's slot.  All lanes call.
@@ -74,14 +80,58 @@ __device__ __forceinline__ uint32_t push(uint32_t* counter, bool want) {
     return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
 }
 
+// Reserves n consecutive slots for each lane; returns the lane's first.  All lanes call.
+__device__ __forceinline__ uint32_t push_n(uint32_t* counter, uint32_t n) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t incl = n;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const uint32_t total = __shfl_sync(kFull, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31u && total) base = atomicAdd(counter, total);
+    return __shfl_sync(kFull, base, 31) + incl - n;
+}
+
+__device__ __forceinline__ uint32_t warp_sum(uint32_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
 enum : int { ACT_NONE_ = 0, ACT_VIS = 1, ACT_THR = 2 };
 
-// Throughput lists shorter than this are carried over (k_round), at most this many rounds in a row.
+// How a ray's chain of visibility queries ended (RayState::pad bits 8-15): open (the chain
+// reached its length; the ray marches on if every query is rejected) or the outcome of the
+// march after its last query, applied when every query of the chain is rejected.
+enum : uint32_t { CHAIN_OPEN = 0, CHAIN_DONE = 1, CHAIN_DROPPED = 2, CHAIN_FAIL = 3 };
+
+// Throughput lists shorter than this are carried over (k_round), at most this many rounds in a
+// row (divided by the round's chain length).
 constexpr uint32_t kThrDeferBelow = 32768u;
 constexpr uint32_t kThrDeferRounds = 8u;
 
+// The end of a march that produced no query: the escaped ray's pixel, a dropped ray or a failed
+// traversal.
+__device__ __forceinline__ void march_end(const RenderConsts& C, const RenderBufs& B, const RayState& st, uint32_t ray, uint32_t end) {
+    if (end == CHAIN_DONE) write_escape(C, st, B.image + 3 * (size_t)ray);
+    else if (end == CHAIN_DROPPED) atomicAdd(&B.ctl->dropped, 1u);
+    else atomicOr(B.status, 2u);
+}
+
 // One round for every queued ray (first = true: ray generation, every pixel's ray).
-// Four 256-thread blocks per SM: 64 registers, which the DDA's state fits without spilling.
+//
+// Query chains.  A ray that marches marches up to `chain` visibility queries ahead: query i+1 is
+// the march that follows query i's rejection (from t_min = query i's middle, query i's voxel
+// excluded), exactly the march the ray would make in the next round after that rejection.  The
+// next round applies the chain's values in order and stops at the first accepted one; the later
+// queries of the chain are dropped, with their query counts.  So every ray takes the same steps as
+// with one query per round, in fewer rounds; a chain costs the queries past an acceptance, and
+// k_round sets the chain length from the fraction of accepted values.
+// Four 256-thread blocks per SM at 64 registers (ptxas spills about 30 words; three blocks at
+// 85 registers without spills render the 1024^2 frame no faster).
 __global__ void __launch_bounds__(256, 4) k_step(const __grid_constant__ RenderConsts C, RenderBufs B, int first) {
     const uint32_t round = first ? 0u : B.ctl->round;
     const uint32_t p = (round + 1u) & 1u, q = round & 1u;   // lists read / written
@@ -89,12 +139,17 @@ __global__ void __launch_bounds__(256, 4) k_step(const __grid_constant__ RenderC
     const uint32_t total = first ? C.n_rays : nv + B.ctl->n_thr;
     // the throughput list was not evaluated this round: its rays go unchanged into the next list
     const bool thr_carried = !first && B.ctl->thr_rows == 0u;
+    const uint32_t chain = first ? 1u : max(B.ctl->chain, 1u);
+    const size_t n = C.n_rays;
+    __shared__ uint32_t s_used, s_accepted;   // visibility values applied / accepted by the block
+    if (threadIdx.x == 0) s_used = s_accepted = 0u;
+    __syncthreads();
     for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
         const uint32_t j = base + threadIdx.x;
         const bool valid = j < total;
         int act = ACT_NONE_;
         bool carried = false;
-        uint32_t ray = 0;
+        uint32_t ray = 0, kr = 0, n_used = 0, n_accepted = 0;
         RayState st;
         if (valid) {
             bool march = false;
@@ -107,14 +162,46 @@ __global__ void __launch_bounds__(256, 4) k_step(const __grid_constant__ RenderC
                 B.ray_stats[2 * ray + 1] = 0u;
                 march = true;
             } else if (j < nv) {
-                ray = B.lists[(p * 2 + 0) * C.n_rays + j];
+                ray = B.lists[(p * 2 + 0) * n + j];
                 st = B.rays[ray];
-                const int vr = vis_resolve(C, st, ray, B.vis_out[j]);
+                const uint32_t row0 = B.vis_row0[p * n + j];
+                const uint32_t pending = st.pad & 0xFFu, end = (st.pad >> 8) & 0xFFu;
+                // the chain's last query is the state's own; the earlier ones are in chain_q / chain_t
+                const int32_t li = st.ijk[0], lj = st.ijk[1], lk = st.ijk[2];
+                const float ln = st.tnear, lf = st.tfar;
+                int vr = VIS_REJECT;
+                uint32_t used = 0;
+                while (used < pending && vr == VIS_REJECT) {
+                    if (used + 1u < pending) {
+                        const int4 a = B.chain_q[used * n + ray];
+                        st.ijk[0] = a.x;
+                        st.ijk[1] = a.y;
+                        st.ijk[2] = a.z;
+                        st.tnear = __int_as_float(a.w);
+                        st.tfar = B.chain_t[used * n + ray];
+                    } else {
+                        st.ijk[0] = li;
+                        st.ijk[1] = lj;
+                        st.ijk[2] = lk;
+                        st.tnear = ln;
+                        st.tfar = lf;
+                    }
+                    vr = vis_resolve(C, st, ray, B.vis_out[row0 + used]);
+                    ++used;
+                }
+                n_used = used;
+                n_accepted = vr != VIS_REJECT;
+                st.meta -= (pending - used) << 8;   // the queries past the accepted one are not taken
+                st.pad = 0u;
+                B.ray_stats[2 * ray] += used;
                 if (vr == VIS_ACCEPT_THR) act = ACT_THR;
-                march = vr == VIS_REJECT;
+                else if (vr == VIS_REJECT) {
+                    if (end == CHAIN_OPEN) march = true;
+                    else march_end(C, B, st, ray, end);
+                }
             } else {
                 const uint32_t jj = j - nv;
-                ray = B.lists[(p * 2 + 1) * C.n_rays + jj];
+                ray = B.lists[(p * 2 + 1) * n + jj];
                 st = B.rays[ray];
                 if (thr_carried) {
                     act = ACT_THR;
@@ -125,50 +212,103 @@ __global__ void __launch_bounds__(256, 4) k_step(const __grid_constant__ RenderC
                 }
             }
             if (march) {
-                const int mr = ray_march(C, st, B.image + 3 * (size_t)ray);
-                if (mr == MARCH_DROPPED) atomicAdd(&B.ctl->dropped, 1u);
-                else if (mr == MARCH_FAIL) atomicOr(B.status, 2u);
-                else if (mr == MARCH_VIS) act = ACT_VIS;
+                st.pad = 0u;
+                for (; kr < chain; ++kr) {
+                    if (kr) st.tmin = past_voxel(st);   // the march after the previous query's rejection
+                    const int mr = march_query(C, st);
+                    if (mr == MARCH_VIS) {
+                        // a query that another one may follow is also kept in chain_q / chain_t
+                        if (kr + 1u < chain) {
+                            B.chain_q[(size_t)kr * C.n_rays + ray] = make_int4(st.ijk[0], st.ijk[1], st.ijk[2], __float_as_int(st.tnear));
+                            B.chain_t[(size_t)kr * C.n_rays + ray] = st.tfar;
+                        }
+                        continue;
+                    }
+                    const uint32_t end = mr == MARCH_DONE ? CHAIN_DONE : mr == MARCH_DROPPED ? CHAIN_DROPPED : CHAIN_FAIL;
+                    if (kr == 0) march_end(C, B, st, ray, end);   // no query pending: the ray ends now
+                    else st.pad = end << 8;
+                    break;
+                }
+                if (kr) {
+                    act = ACT_VIS;
+                    st.pad |= kr;
+                }
             }
         }
         const uint32_t slot_v = push(&B.ctl->cnt[q * 2 + 0], act == ACT_VIS);
+        const uint32_t row_v = push_n(&B.ctl->rows[q], act == ACT_VIS ? kr : 0u);
         const uint32_t slot_t = push(&B.ctl->cnt[q * 2 + 1], act == ACT_THR);
         if (act == ACT_VIS) {
-            B.lists[(q * 2 + 0) * C.n_rays + slot_v] = ray;
-            vis_row(st, B.vis_in + 6 * (size_t)slot_v);
-            B.ray_stats[2 * ray] += 1u;
+            B.lists[(q * 2 + 0) * n + slot_v] = ray;
+            B.vis_row0[q * n + slot_v] = row_v;
+            // the chain's input rows: the earlier queries from chain_q, the last from the state
+            for (uint32_t i = 0; i + 1u < kr; ++i) {
+                const int4 a = B.chain_q[i * n + ray];
+                const int32_t v[3] = {a.x, a.y, a.z};
+                vis_row_at(st, v, __int_as_float(a.w), B.vis_in + 6 * (size_t)(row_v + i));
+            }
+            vis_row(st, B.vis_in + 6 * (size_t)(row_v + kr - 1u));
         } else if (act == ACT_THR) {
-            B.lists[(q * 2 + 1) * C.n_rays + slot_t] = ray;
+            B.lists[(q * 2 + 1) * n + slot_t] = ray;
             thr_row(C, st, B.thr_in + 10 * (size_t)slot_t);
             if (!carried) B.ray_stats[2 * ray + 1] += 1u;
         }
         if (valid) B.rays[ray] = st;
+        n_used = warp_sum(n_used);
+        n_accepted = warp_sum(n_accepted);
+        if ((threadIdx.x & 31u) == 0u && n_used) {
+            atomicAdd(&s_used, n_used);
+            atomicAdd(&s_accepted, n_accepted);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_used) {
+        atomicAdd(&B.ctl->consumed, s_used);
+        atomicAdd(&B.ctl->accepted, s_accepted);
     }
 }
 
-// Publishes the lists built this round, resets the other parity, sets the loop condition.
+// Publishes the lists built this round, resets the other parity, sets the next round's chain
+// length and the loop condition.
 // use_cond: the launch is the loop body's (graph form): it sets the loop condition and the
 // condition of the next round's throughput inference (skipped in rounds that carry the list over
 // or have none).
-__global__ void k_round(Control* ctl, uint32_t max_rounds, uint32_t* status, cudaGraphConditionalHandle cond,
+__global__ void k_round(Control* ctl, uint32_t max_rounds, uint32_t max_chain, uint32_t* status, cudaGraphConditionalHandle cond,
                         cudaGraphConditionalHandle thr_cond, int use_cond) {
     const uint32_t q = ctl->round & 1u;
     const uint32_t nv = ctl->cnt[q * 2 + 0], nt = ctl->cnt[q * 2 + 1];
+    // Chain length: the queries past an accepted one are evaluated for nothing.  With a fraction a
+    // of accepted values, a chain of c queries evaluates about (c - 1) a / 2 of them in vain; the
+    // chain is the longest power of two up to max_chain that keeps this at 1/32, from the last
+    // round's values (kept when that round resolved too few to tell).
+    const uint32_t used = ctl->consumed, acc = ctl->accepted;
+    uint32_t chain = ctl->chain ? ctl->chain : 1u;
+    if (used >= 1024u) {
+        chain = 1u;
+        while (chain * 2u <= max_chain && (uint64_t)(chain * 2u - 1u) * acc * 16u <= used) chain *= 2u;
+    }
+    ctl->chain = min(chain, max_chain);
+    ctl->tot_vis += used;
+    ctl->consumed = 0u;
+    ctl->accepted = 0u;
     // A short throughput list waits for more rows instead of paying a whole inference launch for a
     // few of them (a launch costs about as much for one tile as for a few hundred): it is carried
-    // into the next round, at most kThrDeferRounds rounds in a row and only while visibility
-    // queries keep the rounds going.  A carried ray's state and queries are unchanged, so every
-    // ray takes the same steps; only the round it takes them in moves.
-    const bool defer = nt > 0u && nt < kThrDeferBelow && nv > 0u && ctl->thr_deferred < kThrDeferRounds;
+    // into the next round, at most kThrDeferRounds / chain rounds in a row and only while
+    // visibility queries keep the rounds going.  A carried ray's state and queries are unchanged,
+    // so every ray takes the same steps; only the round it takes them in moves.
+    const uint32_t defer_rounds = kThrDeferRounds / ctl->chain;
+    const bool defer = nt > 0u && nt < kThrDeferBelow && nv > 0u && ctl->thr_deferred < defer_rounds;
     ctl->n_vis = nv;
     ctl->n_thr = nt;
+    ctl->n_rows = ctl->rows[q];
+    ctl->tot_rows += ctl->rows[q];
     ctl->thr_rows = defer ? 0u : nt;
     ctl->thr_deferred = defer ? ctl->thr_deferred + 1u : 0u;
-    ctl->tot_vis += nv;
     ctl->tot_thr += defer ? 0u : nt;
     ctl->tot_rounds += 1;
     ctl->cnt[(q ^ 1u) * 2 + 0] = 0u;
     ctl->cnt[(q ^ 1u) * 2 + 1] = 0u;
+    ctl->rows[q ^ 1u] = 0u;
     ctl->round += 1u;
     bool more = nv + nt > 0;
     if (more && ctl->round > max_rounds) {
@@ -235,6 +375,7 @@ struct nlod_renderer {
     RenderConsts C{};
     RenderBufs B{};
     uint32_t n_pad = 0;
+    uint32_t vis_rows_max = 0;      // visibility rows of the wavefront forms' buffers
     float vis_max_level = 1000.f;
     int mode = NLOD_RENDER_WAVEFRONT;
     int pk_groups = 0;              // tile pipelines per CTA of the persistent form (autotuned)
@@ -279,6 +420,7 @@ void validate(const nlod_render_params& p) {
     if (p.max_depth == 0 || p.max_depth > 255) throw Error(NLOD_ERR_INVALID, "max_depth must be in [1, 255]");
     if (p.max_vis_queries == 0 || p.max_vis_queries > 65535) throw Error(NLOD_ERR_INVALID, "max_vis_queries must be in [1, 65535]");
     if (!(p.fov_y_deg > 0.f && p.fov_y_deg < 180.f)) throw Error(NLOD_ERR_INVALID, "fov_y_deg must be in (0, 180)");
+    if (p.max_chain > 64) throw Error(NLOD_ERR_INVALID, "max_chain must be in [0, 64]");
 }
 
 }  // namespace
@@ -467,11 +609,18 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
                 return q;
             };
             RenderBufs& B = r->B;
+            // query chains of up to max_chain (0: 8) visibility queries per ray, within 2^23 rows
+            C.max_chain = std::max<uint32_t>(1u, std::min<uint32_t>(p->max_chain ? p->max_chain : 8u, (1u << 23) / r->n_pad));
+            const size_t vis_cap = (size_t)C.max_chain * r->n_pad;
+            r->vis_rows_max = (uint32_t)vis_cap;
             B.rays = static_cast<RayState*>(alloc(sizeof(RayState) * n));
             B.lists = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * 4 * (size_t)n));
             B.ctl = static_cast<Control*>(alloc(sizeof(Control)));
-            B.vis_in = static_cast<float*>(alloc(sizeof(float) * 6 * (size_t)r->n_pad));
-            B.vis_out = static_cast<float*>(alloc(sizeof(float) * (size_t)r->n_pad));
+            B.vis_in = static_cast<float*>(alloc(sizeof(float) * 6 * vis_cap));
+            B.vis_out = static_cast<float*>(alloc(sizeof(float) * vis_cap));
+            B.chain_q = static_cast<int4*>(alloc(sizeof(int4) * C.max_chain * (size_t)n));
+            B.chain_t = static_cast<float*>(alloc(sizeof(float) * C.max_chain * (size_t)n));
+            B.vis_row0 = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * 2 * (size_t)n));
             B.thr_in = static_cast<float*>(alloc(sizeof(float) * 10 * (size_t)r->n_pad));
             B.thr_out = static_cast<float*>(alloc(sizeof(float) * 3 * (size_t)r->n_pad));
             B.image = static_cast<float*>(alloc(sizeof(float) * 3 * (size_t)n));
@@ -481,7 +630,7 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             cudaStream_t s = r->cap_stream;
             // One launch of each inference with zero rows (outside any capture): sets the kernels'
             // shared-memory attributes before the graph is recorded.
-            cuda_check(module_inference_device_count(r->vis, r->n_pad, B.vis_in, B.vis_out, &B.ctl->n_vis, r->vis_max_level, s), "inference");
+            cuda_check(module_inference_device_count(r->vis, r->vis_rows_max, B.vis_in, B.vis_out, &B.ctl->n_rows, r->vis_max_level, s), "inference");
             cuda_check(module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, s), "inference");
             cuda_check(cudaStreamSynchronize(s), "synchronize");
 
@@ -492,7 +641,7 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
             k_reset<<<1, 1, 0, s>>>(B.ctl);
             k_step<<<blocks, 256, 0, s>>>(C, B, 1);
-            k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, B.status, 0, 0, 0);
+            k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, C.max_chain, B.status, 0, 0, 0);
             cudaStreamCaptureStatus cst;
             cudaGraph_t cap_graph = nullptr;
             const cudaGraphNode_t* deps = nullptr;
@@ -513,7 +662,7 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             cuda_check(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking), "stream");
             cudaError_t e = cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
-                e = module_inference_device_count(r->vis, r->n_pad, B.vis_in, B.vis_out, &B.ctl->n_vis, r->vis_max_level, bs);
+                e = module_inference_device_count(r->vis, r->vis_rows_max, B.vis_in, B.vis_out, &B.ctl->n_rows, r->vis_max_level, bs);
                 // the throughput inference inside an if node: most rounds carry its list over (or
                 // have none), and a launch that finds no rows still costs its grid's start-up
                 cudaGraphConditionalHandle thr_cond{};
@@ -522,7 +671,7 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
                 });
                 if (e == cudaSuccess) {
                     k_step<<<blocks, 256, 0, bs>>>(C, B, 0);
-                    k_round<<<1, 1, 0, bs>>>(B.ctl, C.max_rounds, B.status, cond, thr_cond, 1);
+                    k_round<<<1, 1, 0, bs>>>(B.ctl, C.max_rounds, C.max_chain, B.status, cond, thr_cond, 1);
                     e = cudaGetLastError();
                 }
                 cudaGraph_t body_out = body;
@@ -554,17 +703,17 @@ int nlod_render_frame(nlod_renderer* r, void* stream, float* image, uint32_t* ra
             const RenderConsts& C = r->C;
             k_reset<<<1, 1, 0, s>>>(B.ctl);
             k_step<<<r->step_blocks, 256, 0, s>>>(C, B, 1);
-            k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, B.status, 0, 0, 0);
+            k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, C.max_chain, B.status, 0, 0, 0);
             cuda_check(cudaGetLastError(), "launch");
             for (;;) {
                 Control c;
                 cuda_check(cudaMemcpyAsync(&c, B.ctl, sizeof c, cudaMemcpyDeviceToHost, s), "copy");
                 cuda_check(cudaStreamSynchronize(s), "synchronize");
                 if (c.n_vis + c.n_thr == 0 || c.round > C.max_rounds) break;
-                cuda_check(module_inference_device_count(r->vis, r->n_pad, B.vis_in, B.vis_out, &B.ctl->n_vis, r->vis_max_level, s), "inference");
+                cuda_check(module_inference_device_count(r->vis, r->vis_rows_max, B.vis_in, B.vis_out, &B.ctl->n_rows, r->vis_max_level, s), "inference");
                 cuda_check(module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, s), "inference");
                 k_step<<<r->step_blocks, 256, 0, s>>>(C, B, 0);
-                k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, B.status, 0, 0, 0);
+                k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, C.max_chain, B.status, 0, 0, 0);
                 cuda_check(cudaGetLastError(), "launch");
             }
         } else {

@@ -1,5 +1,5 @@
 // Per-ray state and per-ray steps of the neural-LoD render query, shared by the wavefront form
-// (render.cu: one query per ray per round, rounds in a conditional graph loop) and the persistent
+// (render.cu: rounds in a conditional graph loop, a chain of queries per ray and round) and the persistent
 // form (render_pk.cu: tile pipelines that refill their ray slots from a global queue).  Both forms
 // call these functions, so a ray takes the same steps with the same roundings in either.
 //
@@ -52,6 +52,7 @@ struct RenderConsts {
     uint32_t seed_lo, seed_hi;
     uint32_t budget;
     uint32_t max_rounds;
+    uint32_t max_chain;   // wavefront form: longest chain of visibility queries a ray marches ahead
 };
 
 // Control words: [0..3] list counters [parity * 2 + kind] (the persistent form uses [0] as its
@@ -59,12 +60,16 @@ struct RenderConsts {
 // [7] rays dropped at the per-bounce query cap; then 64-bit totals: visibility queries,
 // throughput queries, rounds (the persistent form: the most tile iterations of any pipeline);
 // then the wavefront form's throughput rows evaluated this round (0 while a short list is
-// carried over) and the rounds the list has been carried over in a row.
+// carried over) and the rounds the list has been carried over in a row; its visibility row
+// counters [parity], the rows of the current round, the chain length of the next round, the
+// visibility results consumed and accepted in the last round, and the total rows evaluated.
 struct Control {
     uint32_t cnt[4];
     uint32_t n_vis, n_thr, round, dropped;
     unsigned long long tot_vis, tot_thr, tot_rounds;
     uint32_t thr_rows, thr_deferred;
+    uint32_t rows[2], n_rows, chain, consumed, accepted;
+    unsigned long long tot_rows;
 };
 
 __device__ __forceinline__ uint32_t mix32(uint32_t h) {
@@ -126,10 +131,6 @@ __device__ __forceinline__ void ray_generate(const RenderConsts& C, uint32_t j, 
 
 enum : int { MARCH_DONE = 0, MARCH_VIS = 1, MARCH_FAIL = 2, MARCH_DROPPED = 3 };
 
-// Marches to the next occupied voxel.  MARCH_VIS: the ray's next visibility query is set up
-// (voxel, t_near / t_far, query count).  MARCH_DONE: the ray escaped and its pixel is written
-// (background before the first bounce, environment times throughput after).  MARCH_DROPPED: the
-// per-bounce query cap was reached.  MARCH_FAIL: the DDA ran out of its step budget.
 // The pixel of a ray that escaped: the background before the first bounce, the environment
 // times the path throughput after.
 __device__ __forceinline__ void write_escape(const RenderConsts& C, const RayState& st, float* __restrict__ pixel) {
@@ -138,17 +139,18 @@ __device__ __forceinline__ void write_escape(const RenderConsts& C, const RaySta
     for (int k = 0; k < 3; ++k) pixel[k] = bounce == 0 ? C.background[k] : __fmul_rn(st.tp[k], C.env[k]);
 }
 
-__device__ __forceinline__ int ray_march(const RenderConsts& C, RayState& st, float* __restrict__ pixel) {
+// Marches to the next occupied voxel.  MARCH_VIS: the ray's next visibility query is set up
+// (voxel, t_near / t_far, query count).  MARCH_DONE: the ray escaped (the caller writes its
+// pixel).  MARCH_DROPPED: the per-bounce query cap was reached.  MARCH_FAIL: the DDA ran out of
+// its step budget.
+__device__ __forceinline__ int march_query(const RenderConsts& C, RayState& st) {
     const uint32_t nvis = (st.meta >> 8) & 0xFFFFu;
     if (nvis >= C.max_vis) return MARCH_DROPPED;
     int32_t v3[3] = {0, 0, 0};
     float tn = 0.f, tf = 0.f;
     const int r = dda::first_active_voxel(C.L, st.o, st.d, st.tmin, st.ijk, v3, tn, tf, C.budget);
     if (r < 0) return MARCH_FAIL;
-    if (r == 0) {
-        write_escape(C, st, pixel);
-        return MARCH_DONE;
-    }
+    if (r == 0) return MARCH_DONE;
 #pragma unroll
     for (int k = 0; k < 3; ++k) st.ijk[k] = v3[k];
     st.tnear = tn;
@@ -157,7 +159,17 @@ __device__ __forceinline__ int ray_march(const RenderConsts& C, RayState& st, fl
     return MARCH_VIS;
 }
 
+// march_query, with the pixel of an escaped ray written.
+__device__ __forceinline__ int ray_march(const RenderConsts& C, RayState& st, float* __restrict__ pixel) {
+    const int r = march_query(C, st);
+    if (r == MARCH_DONE) write_escape(C, st, pixel);
+    return r;
+}
+
 enum : int { VIS_REJECT = 0, VIS_ACCEPT_THR = 1, VIS_ACCEPT_END = 2 };
+
+// The ray parameter a rejected voxel's march restarts from: the voxel's middle.
+__device__ __forceinline__ float past_voxel(const RayState& st) { return __fmul_rn(__fadd_rn(st.tnear, st.tfar), 0.5f); }
 
 // Applies a visibility value: rejected -> the ray continues past the voxel (tmin moved to the
 // voxel's middle; the caller marches); accepted -> a throughput query with a sampled incoming
@@ -171,7 +183,7 @@ __device__ __forceinline__ int vis_resolve(const RenderConsts& C, RayState& st, 
         }
         return VIS_ACCEPT_END;
     }
-    st.tmin = __fmul_rn(__fadd_rn(st.tnear, st.tfar), 0.5f);
+    st.tmin = past_voxel(st);
     return VIS_REJECT;
 }
 
@@ -195,14 +207,17 @@ __device__ __forceinline__ bool thr_resolve(RayState& st, const float (&t)[3]) {
 }
 
 // Network input rows of a ray's pending query.
-__device__ __forceinline__ void vis_row(const RayState& st, float* __restrict__ row) {
+// (the query in voxel ijk entered at t_near)
+__device__ __forceinline__ void vis_row_at(const RayState& st, const int32_t (&ijk)[3], float t_near, float* __restrict__ row) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const float pk = __fadd_rn(st.o[k], __fmul_rn(st.d[k], st.tnear));
-        row[k] = fminf(fmaxf(__fsub_rn(pk, (float)st.ijk[k]), 0.f), 1.f);
+        const float pk = __fadd_rn(st.o[k], __fmul_rn(st.d[k], t_near));
+        row[k] = fminf(fmaxf(__fsub_rn(pk, (float)ijk[k]), 0.f), 1.f);
         row[3 + k] = __fmul_rn(__fadd_rn(st.d[k], 1.f), 0.5f);
     }
 }
+
+__device__ __forceinline__ void vis_row(const RayState& st, float* __restrict__ row) { vis_row_at(st, st.ijk, st.tnear, row); }
 
 __device__ __forceinline__ void thr_row(const RenderConsts& C, const RayState& st, float* __restrict__ row) {
 #pragma unroll

@@ -24,7 +24,8 @@ class _Params(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("level", C.c_uint32), ("max_depth", C.c_uint32),
                 ("max_vis_queries", C.c_uint32), ("threshold", C.c_float), ("eye", C.c_float * 3), ("target", C.c_float * 3),
                 ("up", C.c_float * 3), ("fov_y_deg", C.c_float), ("background", C.c_float * 3), ("env_color", C.c_float * 3),
-                ("lod_max_level", C.c_float), ("lod_input", C.c_float), ("seed", C.c_uint64), ("mode", C.c_uint32)]
+                ("lod_max_level", C.c_float), ("lod_input", C.c_float), ("seed", C.c_uint64), ("mode", C.c_uint32),
+                ("max_chain", C.c_uint32)]
 
 MODE_AUTO, MODE_WAVEFRONT, MODE_PERSISTENT, MODE_HOST_ROUNDS = 0, 1, 2, 3     # NLOD_RENDER_*
 
@@ -52,12 +53,13 @@ class RenderParams:
     lod_input: float = 0.0
     seed: int = 1337
     mode: int = MODE_AUTO
+    max_chain: int = 0      # most visibility queries a ray marches ahead per round (0: 8)
     extra: dict = field(default_factory=dict)
 
     def to_c(self) -> _Params:
         p = _Params()
         for k in ("width", "height", "level", "max_depth", "max_vis_queries", "threshold", "fov_y_deg", "lod_max_level",
-                  "lod_input", "seed", "mode"):
+                  "lod_input", "seed", "mode", "max_chain"):
             setattr(p, k, getattr(self, k))
         for k in ("eye", "target", "up", "background", "env_color"):
             getattr(p, k)[:] = [float(v) for v in getattr(self, k)]

@@ -150,3 +150,28 @@ def test_persistent_form_needs_tensor_core_modules(cuda, nlod_lib):
     vm, tm, *_ = _nets("fp32")
     with pytest.raises(NlodError):
         Renderer(vm, tm, grid, RenderParams(width=32, height=32, level=1, mode=MODE_PERSISTENT))
+
+
+@pytest.mark.parametrize("precision", ["fp16", "fp32"])
+@pytest.mark.parametrize("threshold,cap", [(0.5, 24), (0.8, 24), (0.8, 7)])
+def test_query_chains_match_single_queries(cuda, nlod_lib, precision, threshold, cap):
+    """Wavefront rounds with chains of visibility queries marched ahead (max_chain 0: up to 8, and
+    3) against one query per ray and round (max_chain 1): the same pixels, per-ray query counts and
+    totals; a threshold that rejects most voxels makes the chains long (fewer rounds), and a small
+    per-bounce cap drops rays inside chains."""
+    bits, res, levels = _scene()
+    grid = LodGrid(bits, res, levels)
+    params = RenderParams(width=96, height=64, level=1, max_depth=4, max_vis_queries=cap, lod_max_level=6 / 8, lod_input=1.5 / 8,
+                          threshold=threshold)
+    img1, st1, tot1 = _frame(precision, RenderParams(**{**params.__dict__, "max_chain": 1}), grid, MODE_WAVEFRONT)
+    for mc in (0, 3):
+        img, st, tot = _frame(precision, RenderParams(**{**params.__dict__, "max_chain": mc}), grid, MODE_WAVEFRONT)
+        print(f"{precision} threshold {threshold} cap {cap} max_chain {mc}: totals {tot}, one query per round {tot1}")
+        assert np.array_equal(st, st1)
+        assert np.array_equal(img.view(np.uint32), img1.view(np.uint32))
+        assert tot[0] == tot1[0] and tot[1] == tot1[1] and tot[3] == tot1[3]
+        assert tot[2] <= tot1[2]
+        if threshold == 0.8:
+            assert tot[2] < tot1[2]
+    if cap == 7:
+        assert tot1[3] > 0
