@@ -220,8 +220,10 @@ NLOD_API void nlod_free_string(char* s);
 /*
  * Kernel organisation of the tensor-core query (tile pipelines per CTA x grid levels per gather
  * unit).  No tiny-cuda-nn counterpart (its launch shapes are fixed).  nlod_autotune times every
- * variant that fits the network on the given batch (synchronous, runs the query 4 times per
- * variant) and keeps the fastest; nlod_set_kernel_variant forces one.  The FP32 form has one.
+ * variant that fits the network on the given batch and keeps the fastest (synchronous; per variant
+ * one warm-up and three timed launches in rounds over all variants, each timed launch after a
+ * write of twice the L2's size to a scratch buffer allocated for the call, the median deciding);
+ * nlod_set_kernel_variant forces one.  The FP32 form has one.
  */
 NLOD_API int nlod_kernel_variants(const nlod_module* m);
 NLOD_API int nlod_get_kernel_variant(const nlod_module* m);

@@ -7,6 +7,7 @@
 #include <functional>
 #include <cstdint>
 #include <cstdio>
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -70,6 +71,14 @@ struct nlod_module {
     void* w_op = nullptr;           // operand copy (FP16/BF16) of the network part of `params`
     void* w_op_inf = nullptr;       // operand copy of the inference network weights
     uint16_t* grid_h = nullptr;     // FP16 copy of the inference parameters (grid part used), FP16 modules with grids
+    // Cell table of grid_h's leading dense levels (cells.cu).  An optimizer step marks it out of
+    // date on the device (cells_stale, which the kernels read before using it) and on the host
+    // (cells_dirty); the next inference call rebuilds it, so training steps do not pay for it and
+    // captured inference stays correct (it gathers while the table is out of date).
+    void* cells = nullptr;
+    uint32_t cells_levels = 0;
+    uint32_t* cells_stale = nullptr;
+    bool cells_dirty = false;
     uint16_t* grid_h_train = nullptr;  // FP16 copy of the training values (grid part), FP16 modules with grids and an EMA
     uint32_t* status = nullptr;     // device status word (bounded-wait timeouts)
 
@@ -132,6 +141,14 @@ void check_batch(uint32_t n) {
         throw Error(NLOD_ERR_INVALID, "batch size must be a multiple of 128 (got " + std::to_string(n) + ")");
 }
 
+// Rebuilds the cell table when an optimizer step has changed the FP16 tables since the last build.
+void ensure_cells(nlod_module* m, cudaStream_t s) {
+    if (!m->cells || !m->cells_dirty) return;
+    cuda_check(launch_build_cells(m->d, m->grid_h, m->cells_levels, m->cells, s), "cell table");
+    cuda_check(cudaMemsetAsync(m->cells_stale, 0, sizeof(uint32_t), s), "cell table");
+    m->cells_dirty = false;
+}
+
 // Derived copies of the parameters after they were set from outside (an optimizer step refreshes
 // them in its own pass).
 void refresh_operand_copies(nlod_module* m, cudaStream_t s) {
@@ -146,6 +163,8 @@ void refresh_operand_copies(nlod_module* m, cudaStream_t s) {
         cuda_check(launch_convert_weights(m->inference_params() + off, m->grid_h + off, n, 1, s), "convert grid tables");
         if (m->grid_h_train)
             cuda_check(launch_convert_weights(m->params + off, m->grid_h_train + off, n, 1, s), "convert grid tables");
+        m->cells_dirty = m->cells != nullptr;
+        ensure_cells(m, s);
     }
 }
 
@@ -156,6 +175,9 @@ ForwardArgs base_forward_args(nlod_module* m, uint32_t n, const float* in, bool 
     a.params = inference ? m->inference_params() : m->params;
     a.weights_op = inference ? m->w_op_inf : m->w_op;
     a.grid_h = inference ? m->grid_h : nullptr;
+    a.cells = inference ? m->cells : nullptr;
+    a.cells_levels = inference ? m->cells_levels : 0u;
+    a.cells_stale = m->cells_stale;
     a.max_level_gpu = m->max_level_gpu;
     a.max_level = m->max_level;
     return a;
@@ -255,7 +277,9 @@ void run_optimizer(nlod_module* m, cudaStream_t s) {
     a.w_op = m->precision == NLOD_PRECISION_FP32 ? nullptr : m->w_op;
     a.w_op_inf = m->precision == NLOD_PRECISION_FP32 ? nullptr : m->w_op_inf;
     a.op_kind = m->op_kind();
+    a.cells_stale = m->cells_stale;
     cuda_check(launch_adam_step(a, s), "adam step");
+    m->cells_dirty = m->cells != nullptr;
 }
 
 void init_params(nlod_module* m, uint64_t seed) {
@@ -289,6 +313,17 @@ cudaError_t module_inference_device_count(nlod_module* m, uint32_t n_max, const 
 }
 
 uint32_t* module_status_word(nlod_module* m) { return m->status; }
+
+// Before inference that a graph captured earlier runs (the renderer's frame): derived tables that
+// lag the parameters are rebuilt on the stream.
+cudaError_t module_prepare_inference(nlod_module* m, cudaStream_t s) {
+    try {
+        ensure_cells(m, s);
+    } catch (const Error&) {
+        return cudaErrorUnknown;
+    }
+    return cudaSuccess;
+}
 
 // Inference operands of a tensor-core module for the persistent renderer: its description, the
 // inference weights in the operand type and the parameter vector its encoding gathers (FP16 copy
@@ -392,6 +427,12 @@ int nlod_module_create(const char* encoding_json, const char* network_json, cons
             if (precision == NLOD_PRECISION_FP16 && m->d.n_grids > 0) {
                 m->grid_h = dev_alloc<uint16_t>(np);
                 if (m->ema) m->grid_h_train = dev_alloc<uint16_t>(np);
+                m->cells_levels = cells_levels_of(m->d);
+                if (m->cells_levels) {
+                    m->cells = dev_alloc<uint8_t>(32u * cells_records(m->d, m->cells_levels));
+                    m->cells_stale = dev_alloc<uint32_t>(1);
+                    cuda_check(cudaMemset(m->cells_stale, 0xFF, sizeof(uint32_t)), "memset");
+                }
             }
             init_params(m.get(), seed);
             refresh_operand_copies(m.get(), 0);
@@ -491,6 +532,8 @@ void nlod_module_destroy(nlod_module* m) {
     if (m->w_op_inf != m->w_op) dev_free(m->w_op_inf);
     dev_free(m->grid_h);
     dev_free(m->grid_h_train);
+    dev_free(m->cells);
+    dev_free(m->cells_stale);
     dev_free(m->w_op);
     dev_free(m->status);
     dev_free(m->loss_partial);
@@ -531,6 +574,7 @@ int nlod_inference(nlod_module* m, void* stream, uint32_t n, const float* in, fl
         if (n == 0) return;
         if (!in || !out) throw Error(NLOD_ERR_INVALID, "input and output must not be NULL");
         cudaStream_t s = (cudaStream_t)stream;
+        ensure_cells(m, s);
         ForwardArgs a = base_forward_args(m, n, in, true);
         a.out = out;
         if (m->precision == NLOD_PRECISION_FP32) cuda_check(launch_forward_simt(m->d, a, 0, s), "inference");
@@ -577,6 +621,7 @@ int nlod_inference_host(nlod_module* m, void* stream, uint32_t n, const float* h
             cuda_check(cudaMemcpyAsync(stage, host_in, in_bytes, cudaMemcpyHostToDevice, s), "input copy");
             in_dev = stage;
         }
+        ensure_cells(m, s);
         ForwardArgs a = base_forward_args(m, n, in_dev, true);
         a.out = out_dev;
         if (m->precision == NLOD_PRECISION_FP32) cuda_check(launch_forward_simt(m->d, a, 0, s), "inference");
@@ -1053,26 +1098,55 @@ int nlod_autotune(nlod_module* m, void* stream, uint32_t n, const float* in, flo
         if (n == 0 || m->precision == NLOD_PRECISION_FP32) return;
         if (!in || !out) throw Error(NLOD_ERR_INVALID, "input and output must not be NULL");
         cudaStream_t s = (cudaStream_t)stream;
-        cudaEvent_t e0, e1;
-        cuda_check(cudaEventCreate(&e0), "event");
-        cuda_check(cudaEventCreate(&e1), "event");
-        float best = 3.0e38f;
-        int best_v = m->tc_variant;
+        ensure_cells(m, s);
         ForwardArgs a = base_forward_args(m, n, in, true);
         a.out = out;
-        for (int v = 0; v < tc_num_variants(); ++v) {
-            if (!tc_variant_ok(m->d, v, m->op_kind())) continue;
-            cuda_check(launch_forward_tc(m->d, a, m->op_kind(), v, m->status, s), "autotune");
-            cuda_check(cudaEventRecord(e0, s), "event");
-            for (int it = 0; it < 3; ++it) cuda_check(launch_forward_tc(m->d, a, m->op_kind(), v, m->status, s), "autotune");
-            cuda_check(cudaEventRecord(e1, s), "event");
-            cuda_check(cudaEventSynchronize(e1), "event");
-            float ms = 0.f;
-            cuda_check(cudaEventElapsedTime(&ms, e0, e1), "event");
-            if (ms < best) { best = ms; best_v = v; }
+        // Each organisation is timed on single launches that find the L2 holding other data (a
+        // scratch write of twice the L2's size before each), in three rounds over all of them; the
+        // median of an organisation's three decides.  Without the scratch (allocation refused) the
+        // launches run back to back.
+        int dev = 0, l2 = 0;
+        cuda_check(cudaGetDevice(&dev), "device");
+        cuda_check(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev), "device");
+        void* scratch = nullptr;
+        const size_t scratch_bytes = 2u * (size_t)(l2 > 0 ? l2 : 0);
+        if (scratch_bytes && cudaMalloc(&scratch, scratch_bytes) != cudaSuccess) {
+            (void)cudaGetLastError();
+            scratch = nullptr;
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        std::vector<int> cand;
+        for (int v = 0; v < tc_num_variants(); ++v)
+            if (tc_variant_ok(m->d, v, m->op_kind())) cand.push_back(v);
+        std::vector<float> times(cand.size() * 3u, 0.f);
+        cudaError_t e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+        for (size_t i = 0; i < cand.size() && e == cudaSuccess; ++i)   // warm-up (also sets each kernel's attributes)
+            e = launch_forward_tc(m->d, a, m->op_kind(), cand[i], m->status, s);
+        for (int round = 0; round < 3 && e == cudaSuccess; ++round) {
+            for (size_t i = 0; i < cand.size() && e == cudaSuccess; ++i) {
+                if (scratch) e = cudaMemsetAsync(scratch, round + 1, scratch_bytes, s);
+                if (e == cudaSuccess) e = cudaEventRecord(e0, s);
+                if (e == cudaSuccess) e = launch_forward_tc(m->d, a, m->op_kind(), cand[i], m->status, s);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&times[i * 3u + round], e0, e1);
+            }
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (scratch) cudaFree(scratch);
+        cuda_check(e, "autotune");
+        float best = 3.0e38f;
+        int best_v = m->tc_variant;
+        for (size_t i = 0; i < cand.size(); ++i) {
+            float t[3] = {times[i * 3u], times[i * 3u + 1u], times[i * 3u + 2u]};
+            std::sort(t, t + 3);
+            if (t[1] < best) {
+                best = t[1];
+                best_v = cand[i];
+            }
+        }
         m->tc_variant = best_v;
     });
 }
@@ -1086,7 +1160,8 @@ int nlod_calib_gathers(nlod_module* m, void* stream, uint32_t n, float* ms_out) 
         // which the next training step clears) only if it equals a value no table sum takes
         const bool half = m->grid_h != nullptr;
         const void* tables = half ? static_cast<const void*>(m->grid_h) : static_cast<const void*>(m->inference_params());
-        time_on_stream(s, ms_out, [&] { return launch_calib_gathers(m->d, tables, half, n, m->grads, s); });
+        ensure_cells(m, s);
+        time_on_stream(s, ms_out, [&] { return launch_calib_gathers(m->d, tables, half, n, m->grads, s, half ? m->cells : nullptr, m->cells_levels); });
     });
 }
 

@@ -1,8 +1,9 @@
 // Calibration kernels: the two memory-side floors of the hot path, measured on a module's own
 // grid with nothing else in the kernel.
 //   k_calib_gathers     the encoding's grid gathers of n queries (grid_group_forward of every grid
-//                       slot, from the FP16 copy of the tables when the module keeps one) at full
-//                       occupancy: the floor of the query kernel and of the training encoding.
+//                       slot, from the FP16 copy of the tables and its cell table when the module
+//                       keeps them) at full occupancy: the floor of the query kernel and of the
+//                       training encoding.
 //   k_calib_scatter     the grid-gradient scatter of n samples (grid_level_scatter8 of every level,
 //                       one FP32x2 or paired FP32x4 reduction per corner), the floor of the fused
 //                       training kernel.
@@ -34,7 +35,7 @@ __device__ __forceinline__ float calib_u01(uint32_t i, uint32_t k) { return (flo
 
 template <typename TT>
 __global__ void __launch_bounds__(kCalibThreads) k_calib_gathers(const __grid_constant__ ModelDesc d, const TT* __restrict__ params, uint32_t n,
-                                                                 float* __restrict__ sink) {
+                                                                 float* __restrict__ sink, const uint4* __restrict__ cells, uint32_t cells_levels) {
     __shared__ GridLevel lvl[kMaxGrids * kMaxLevels];
     for (uint32_t i = threadIdx.x; i < d.n_grids * (uint32_t)kMaxLevels; i += blockDim.x) {
         const uint32_t g = i / kMaxLevels, l = i % kMaxLevels;
@@ -51,7 +52,8 @@ __global__ void __launch_bounds__(kCalibThreads) k_calib_gathers(const __grid_co
 #pragma unroll 1
             for (uint32_t l = 0; l < g.n_levels; ++l) {
                 float f[2];
-                grid_group_forward<1, TT>(g, lvl + s.grid * kMaxLevels, l, 1u, params + g.param_offset, px, py, pz, 1000.f, f);
+                grid_group_forward<1, TT>(g, lvl + s.grid * kMaxLevels, l, 1u, params + g.param_offset, px, py, pz, 1000.f, f, nullptr, 0u,
+                                          cells, s.grid == 0 ? cells_levels : 0u);
                 acc += f[0] + f[1];
             }
         }
@@ -90,7 +92,8 @@ __global__ void __launch_bounds__(kCalibThreads) k_calib_scatter(const __grid_co
 
 }  // namespace
 
-cudaError_t launch_calib_gathers(const ModelDesc& d, const void* params, bool half_tables, uint32_t n, float* sink, cudaStream_t s) {
+cudaError_t launch_calib_gathers(const ModelDesc& d, const void* params, bool half_tables, uint32_t n, float* sink, cudaStream_t s,
+                                 const void* cells, uint32_t cells_levels) {
     int sms = 0, dev = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -99,8 +102,11 @@ cudaError_t launch_calib_gathers(const ModelDesc& d, const void* params, bool ha
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCalibThreads, 0);
     if (e != cudaSuccess) return e;
     const uint32_t blocks = (uint32_t)(sms * (per_sm > 0 ? per_sm : 1));
-    if (half_tables) k_calib_gathers<__half><<<blocks, kCalibThreads, 0, s>>>(d, static_cast<const __half*>(params), n, sink);
-    else k_calib_gathers<float><<<blocks, kCalibThreads, 0, s>>>(d, static_cast<const float*>(params), n, sink);
+    if (half_tables)
+        k_calib_gathers<__half><<<blocks, kCalibThreads, 0, s>>>(d, static_cast<const __half*>(params), n, sink, static_cast<const uint4*>(cells),
+                                                                 cells ? cells_levels : 0u);
+    else
+        k_calib_gathers<float><<<blocks, kCalibThreads, 0, s>>>(d, static_cast<const float*>(params), n, sink, nullptr, 0u);
     return cudaGetLastError();
 }
 

@@ -68,6 +68,7 @@ __device__ __forceinline__ void store_op1(void* dst, uint32_t i, float v, int ki
 __global__ void __launch_bounds__(256) k_adam_step(const __grid_constant__ AdamStepArgs a) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t i0 = 4u * q;
+    if (q == 0 && a.cells_stale) *a.cells_stale = 1u;
     if (i0 >= a.n_params) return;
     if (i0 + 4u <= a.n_params) {
         float4 w = reinterpret_cast<const float4*>(a.params)[q];

@@ -48,6 +48,7 @@ namespace nlod {
 cudaError_t module_inference_device_count(nlod_module* m, uint32_t n_max, const float* in, float* out, const uint32_t* n_dev,
                                           float max_level, cudaStream_t s);
 bool module_tc_operands(nlod_module* m, const ModelDesc** d, const void** weights, const void** table, int* kind);
+cudaError_t module_prepare_inference(nlod_module* m, cudaStream_t s);
 
 namespace {
 
@@ -628,6 +629,8 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             B.status = static_cast<uint32_t*>(alloc(sizeof(uint32_t)));
             cuda_check(cudaStreamCreateWithFlags(&r->cap_stream, cudaStreamNonBlocking), "stream");
             cudaStream_t s = r->cap_stream;
+            cuda_check(module_prepare_inference(r->vis, s), "inference tables");
+            cuda_check(module_prepare_inference(r->thr, s), "inference tables");
             // One launch of each inference with zero rows (outside any capture): sets the kernels'
             // shared-memory attributes before the graph is recorded.
             cuda_check(module_inference_device_count(r->vis, r->vis_rows_max, B.vis_in, B.vis_out, &B.ctl->n_rows, r->vis_max_level, s), "inference");
@@ -697,6 +700,9 @@ int nlod_render_frame(nlod_renderer* r, void* stream, float* image, uint32_t* ra
     return guarded([&] {
         if (!r) throw Error(NLOD_ERR_INVALID, "renderer is NULL");
         cudaStream_t s = (cudaStream_t)stream;
+        // tables derived from the modules' parameters (rebuilt when a training step changed them)
+        cuda_check(module_prepare_inference(r->vis, s), "inference tables");
+        cuda_check(module_prepare_inference(r->thr, s), "inference tables");
         if (r->mode == NLOD_RENDER_HOST_ROUNDS) {
             // the graph's rounds, issued from the host: it reads the list sizes after each round
             RenderBufs& B = r->B;

@@ -137,6 +137,29 @@ def test_dense_and_nearest_grids(cuda, nlod_lib):
         _check(out, ref, precision)
 
 
+def test_dense_level_cell_table(cuda, nlod_lib):
+    """The FP16 form reads the corners of a dense level's cell from the cell table (one 32-byte
+    record per cell, rebuilt with the FP16 tables); positions on the grid's far faces (whose
+    corners wrap past the level's last entry), outside [0,1] (no record: the corners are gathered)
+    and inside all match the oracle, and the leading dense levels of a hash grid too."""
+    import torch
+
+    enc = {"otype": "Composite", "nested": [
+        {"otype": "DenseGrid", "n_dims_to_encode": 3, "n_levels": 3, "base_resolution": 6, "per_level_scale": 1.5},
+        {"otype": "Identity", "n_dims_to_encode": 1}]}
+    net = {"otype": "FullyFusedMLP", "n_neurons": 64, "n_hidden_layers": 2, "activation": "ReLU", "output_activation": "None"}
+    rng = np.random.default_rng(12)
+    x = rng.random((2048, 4)).astype(np.float32)
+    x[:256, :3] = rng.integers(0, 2, (256, 3)).astype(np.float32)      # cube corners and faces
+    x[256:512, :3] = x[256:512, :3] * 1.3 - 0.15                        # outside [0,1]
+    for cfg, n_in, xs in (((enc, net), 4, x), (W.throughput_configs(), 10, W.throughput_inputs(2048, seed=13))):
+        m, orc, params = _net(cfg, n_in, 3 if n_in == 10 else 1, "fp16", grid_scale=0.5)
+        ref = orc.forward(xs, params)
+        out = m.inference(torch.from_numpy(xs).to(cuda)).cpu().numpy()
+        m.sync_status()
+        _check(out, ref, "fp16")
+
+
 @pytest.mark.parametrize("precision", ["fp16", "bf16"])
 def test_every_kernel_variant_and_autotune(cuda, nlod_lib, precision):
     """Each tensor-core kernel organisation the autotuner may pick computes the same result."""
@@ -291,3 +314,39 @@ def test_calibration_floors(cuda, nlod_lib):
     loss = m.training_step(x, t).item()
     m.sync_status()
     assert np.isfinite(loss)
+
+
+def test_captured_inference_after_training_without_cell_rebuild(cuda, nlod_lib):
+    """Inference captured in a CUDA graph before training still reads current values when it is
+    replayed after an optimizer step that nothing has rebuilt the cell table for since: the step
+    marks the table out of date on the device and the kernel then gathers the corners."""
+    import torch
+
+    enc, net = W.throughput_configs()
+    opt = W.THROUGHPUT_OPTIMIZER["nested"]["nested"]
+    m = NetworkWithInputEncoding(10, 3, enc, net, loss=W.THROUGHPUT_LOSS, optimizer=opt, precision="fp16")
+    spec = oracle.model_spec(enc, net, 10, 3)
+    m.set_params(W.test_params(spec, seed=5, grid_scale=0.2))
+    x = torch.from_numpy(W.throughput_inputs(4096, seed=11)).to(cuda)
+    t = torch.rand((4096, 3), device=cuda)
+    out = torch.empty((4096, 3), device=cuda)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        m.inference(x, out)                      # cell table current: nothing to rebuild in the capture
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            m.inference(x, out)
+    torch.cuda.synchronize()
+    y0 = out.clone()
+    m.training_step(x, t)
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    m.sync_status()
+    y1 = out.clone()
+    assert not torch.equal(y0, y1)
+    fresh = NetworkWithInputEncoding(10, 3, enc, net, precision="fp16")
+    fresh.set_params(m.get_params("inference"))
+    assert torch.equal(fresh.inference(x), y1)
+    assert torch.equal(m.inference(x), y1)     # rebuilt table, same values
