@@ -71,12 +71,13 @@ struct nlod_module {
     void* w_op = nullptr;           // operand copy (FP16/BF16) of the network part of `params`
     void* w_op_inf = nullptr;       // operand copy of the inference network weights
     uint16_t* grid_h = nullptr;     // FP16 copy of the inference parameters (grid part used), FP16 modules with grids
-    // Cell table of grid_h's leading dense levels (cells.cu).  An optimizer step marks it out of
+    // Cell table of grid_h's leading levels (cells.cu).  An optimizer step marks it out of
     // date on the device (cells_stale, which the kernels read before using it) and on the host
     // (cells_dirty); the next inference call rebuilds it, so training steps do not pay for it and
     // captured inference stays correct (it gathers while the table is out of date).
     void* cells = nullptr;
     uint32_t cells_levels = 0;
+    uint32_t cell_base[kMaxLevels + 1] = {};
     uint32_t* cells_stale = nullptr;
     bool cells_dirty = false;
     uint16_t* grid_h_train = nullptr;  // FP16 copy of the training values (grid part), FP16 modules with grids and an EMA
@@ -144,7 +145,7 @@ void check_batch(uint32_t n) {
 // Rebuilds the cell table when an optimizer step has changed the FP16 tables since the last build.
 void ensure_cells(nlod_module* m, cudaStream_t s) {
     if (!m->cells || !m->cells_dirty) return;
-    cuda_check(launch_build_cells(m->d, m->grid_h, m->cells_levels, m->cells, s), "cell table");
+    cuda_check(launch_build_cells(m->d, m->grid_h, m->cells_levels, m->cell_base, m->cells, s), "cell table");
     cuda_check(cudaMemsetAsync(m->cells_stale, 0, sizeof(uint32_t), s), "cell table");
     m->cells_dirty = false;
 }
@@ -178,6 +179,7 @@ ForwardArgs base_forward_args(nlod_module* m, uint32_t n, const float* in, bool 
     a.cells = inference ? m->cells : nullptr;
     a.cells_levels = inference ? m->cells_levels : 0u;
     a.cells_stale = m->cells_stale;
+    for (uint32_t l = 0; l < (uint32_t)kMaxLevels; ++l) a.cell_base[l] = m->cell_base[l];
     a.max_level_gpu = m->max_level_gpu;
     a.max_level = m->max_level;
     return a;
@@ -427,9 +429,9 @@ int nlod_module_create(const char* encoding_json, const char* network_json, cons
             if (precision == NLOD_PRECISION_FP16 && m->d.n_grids > 0) {
                 m->grid_h = dev_alloc<uint16_t>(np);
                 if (m->ema) m->grid_h_train = dev_alloc<uint16_t>(np);
-                m->cells_levels = cells_levels_of(m->d);
+                m->cells_levels = cells_levels_of(m->d, m->cell_base);
                 if (m->cells_levels) {
-                    m->cells = dev_alloc<uint8_t>(32u * cells_records(m->d, m->cells_levels));
+                    m->cells = dev_alloc<uint8_t>(32u * (size_t)m->cell_base[m->cells_levels]);
                     m->cells_stale = dev_alloc<uint32_t>(1);
                     cuda_check(cudaMemset(m->cells_stale, 0xFF, sizeof(uint32_t)), "memset");
                 }
@@ -1161,7 +1163,7 @@ int nlod_calib_gathers(nlod_module* m, void* stream, uint32_t n, float* ms_out) 
         const bool half = m->grid_h != nullptr;
         const void* tables = half ? static_cast<const void*>(m->grid_h) : static_cast<const void*>(m->inference_params());
         ensure_cells(m, s);
-        time_on_stream(s, ms_out, [&] { return launch_calib_gathers(m->d, tables, half, n, m->grads, s, half ? m->cells : nullptr, m->cells_levels); });
+        time_on_stream(s, ms_out, [&] { return launch_calib_gathers(m->d, tables, half, n, m->grads, s, half ? m->cells : nullptr, m->cells_levels, m->cell_base); });
     });
 }
 

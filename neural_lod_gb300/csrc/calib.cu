@@ -33,9 +33,15 @@ __device__ __forceinline__ uint32_t calib_hash(uint32_t x) {
 
 __device__ __forceinline__ float calib_u01(uint32_t i, uint32_t k) { return (float)(calib_hash(3u * i + k) >> 8) * (1.0f / 16777216.0f); }
 
+struct CellArgs {
+    const uint4* rec;
+    uint32_t levels;
+    uint32_t base[kMaxLevels];
+};
+
 template <typename TT>
 __global__ void __launch_bounds__(kCalibThreads) k_calib_gathers(const __grid_constant__ ModelDesc d, const TT* __restrict__ params, uint32_t n,
-                                                                 float* __restrict__ sink, const uint4* __restrict__ cells, uint32_t cells_levels) {
+                                                                 float* __restrict__ sink, const __grid_constant__ CellArgs cells) {
     __shared__ GridLevel lvl[kMaxGrids * kMaxLevels];
     for (uint32_t i = threadIdx.x; i < d.n_grids * (uint32_t)kMaxLevels; i += blockDim.x) {
         const uint32_t g = i / kMaxLevels, l = i % kMaxLevels;
@@ -53,7 +59,7 @@ __global__ void __launch_bounds__(kCalibThreads) k_calib_gathers(const __grid_co
             for (uint32_t l = 0; l < g.n_levels; ++l) {
                 float f[2];
                 grid_group_forward<1, TT>(g, lvl + s.grid * kMaxLevels, l, 1u, params + g.param_offset, px, py, pz, 1000.f, f, nullptr, 0u,
-                                          cells, s.grid == 0 ? cells_levels : 0u);
+                                          s.grid == 0 ? CellTable{cells.rec, cells.base, cells.levels} : CellTable{});
                 acc += f[0] + f[1];
             }
         }
@@ -93,7 +99,13 @@ __global__ void __launch_bounds__(kCalibThreads) k_calib_scatter(const __grid_co
 }  // namespace
 
 cudaError_t launch_calib_gathers(const ModelDesc& d, const void* params, bool half_tables, uint32_t n, float* sink, cudaStream_t s,
-                                 const void* cells, uint32_t cells_levels) {
+                                 const void* cells, uint32_t cells_levels, const uint32_t* cell_base) {
+    CellArgs ca{};
+    if (half_tables && cells && cell_base) {
+        ca.rec = static_cast<const uint4*>(cells);
+        ca.levels = cells_levels;
+        for (uint32_t l = 0; l < cells_levels && l < (uint32_t)kMaxLevels; ++l) ca.base[l] = cell_base[l];
+    }
     int sms = 0, dev = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -102,11 +114,8 @@ cudaError_t launch_calib_gathers(const ModelDesc& d, const void* params, bool ha
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCalibThreads, 0);
     if (e != cudaSuccess) return e;
     const uint32_t blocks = (uint32_t)(sms * (per_sm > 0 ? per_sm : 1));
-    if (half_tables)
-        k_calib_gathers<__half><<<blocks, kCalibThreads, 0, s>>>(d, static_cast<const __half*>(params), n, sink, static_cast<const uint4*>(cells),
-                                                                 cells ? cells_levels : 0u);
-    else
-        k_calib_gathers<float><<<blocks, kCalibThreads, 0, s>>>(d, static_cast<const float*>(params), n, sink, nullptr, 0u);
+    if (half_tables) k_calib_gathers<__half><<<blocks, kCalibThreads, 0, s>>>(d, static_cast<const __half*>(params), n, sink, ca);
+    else k_calib_gathers<float><<<blocks, kCalibThreads, 0, s>>>(d, static_cast<const float*>(params), n, sink, CellArgs{});
     return cudaGetLastError();
 }
 

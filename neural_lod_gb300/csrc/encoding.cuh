@@ -161,15 +161,23 @@ __device__ __forceinline__ void table_quad(const __half* t, uint32_t a, uint32_t
 // the two features of level l0 + i.  All gathers of the group are issued before any is used.
 // `levels` is the grid's level table (the kernel parameter copy or a shared-memory copy); `table`
 // the grid's parameters (TT = float, or __half for the FP16 copy).
-// `cells` (FP16 tables only; levels below cells_levels; nullptr: none): the level's cell table, which holds the
-// eight corner entries of every cell (cx, cy, cz) < res of a dense level in one 32-byte record at
-// record L.offset + cx + res (cy + res cz) (build_cells); two 16-byte loads of one sector replace
-// the corners' four to eight gathers.  Cells outside [0, res)^3 take the gathers.
+// Cell table of the first grid's leading levels (FP16 tables; cells.cu): for every cell
+// (cx, cy, cz) < res of level l < levels, the FP16 pairs of its eight corner entries in one 32-byte
+// record at record base[l] + cx + res (cy + res cz).  rec == nullptr: no table.
+struct CellTable {
+    const uint4* rec;
+    const uint32_t* base;
+    uint32_t levels;
+};
+
+// `ct` (FP16 tables only): a level the cell table covers reads a cell's eight corners with two
+// 16-byte loads of one sector instead of four to eight gathers; cells outside [0, res)^3 take the
+// gathers.
 template <int NL, typename TT = float>
 __device__ __forceinline__ void grid_group_forward(const GridDesc& g, const GridLevel* __restrict__ levels, uint32_t l0, uint32_t nl,
                                                    const TT* __restrict__ table, float px, float py, float pz, float ml_frac,
                                                    float (&f)[2 * NL], const uint32_t* smem_tab = nullptr, uint32_t smem_levels = 0,
-                                                   const uint4* __restrict__ cells = nullptr, uint32_t cells_levels = 0) {
+                                                   CellTable ct = {}) {
     uint32_t p0, p1, p2;
     hash_primes(g.hash, p0, p1, p2);
     float2 v[NL][8];
@@ -193,8 +201,8 @@ __device__ __forceinline__ void grid_group_forward(const GridDesc& g, const Grid
             bool from_cells = false;
             if constexpr (std::is_same<TT, __half>::value) {
                 const uint32_t res = L.res_flags & kLevelResMask;
-                if (cells != nullptr && l < cells_levels && cx < res && cy < res && cz < res) {
-                    const uint4* cp = cells + 2u * (L.offset + cx + res * (cy + res * cz));
+                if (ct.rec != nullptr && l < ct.levels && cx < res && cy < res && cz < res) {
+                    const uint4* cp = ct.rec + 2u * (ct.base[l] + cx + res * (cy + res * cz));
                     const uint4 q0 = __ldg(cp), q1 = __ldg(cp + 1);
                     const uint32_t w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
 #pragma unroll
@@ -452,8 +460,7 @@ template <int NL, typename Store, typename TT = float>
 __device__ __forceinline__ void encode_tile_rows(const ModelDesc& d, const GridLevel* level_tables, const TT* __restrict__ params,
                                                  const float* in_s, uint32_t in_ld, const float* __restrict__ ml_gpu, float ml_scalar,
                                                  uint32_t row0, uint32_t rows, uint32_t tid, uint32_t nthreads, Store& st,
-                                                 const uint32_t* smem_tab = nullptr, uint32_t smem_levels = 0,
-                                                 const uint4* cells = nullptr, uint32_t cells_levels = 0) {
+                                                 const uint32_t* smem_tab = nullptr, uint32_t smem_levels = 0, CellTable ct = {}) {
     for (uint32_t r = tid; r < rows; r += nthreads) {
         const float* row = in_s + r * in_ld;
         const float ml = ml_gpu ? __ldg(ml_gpu + row0 + r) : ml_scalar;
@@ -470,8 +477,8 @@ __device__ __forceinline__ void encode_tile_rows(const ModelDesc& d, const GridL
                     float f[2 * NL];
                     const uint32_t nl = min((uint32_t)NL, nlev - l0);
                     // the staged levels and the cell table belong to the first grid
-                    grid_group_forward<NL, TT>(g, lv, l0, nl, table, px, py, pz, ml, f, smem_tab, s.grid == 0 ? smem_levels : 0u, cells,
-                                               s.grid == 0 ? cells_levels : 0u);
+                    grid_group_forward<NL, TT>(g, lv, l0, nl, table, px, py, pz, ml, f, smem_tab, s.grid == 0 ? smem_levels : 0u,
+                                               s.grid == 0 ? ct : CellTable{});
                     st.run(r, s.out_begin + 2u * l0, f, 2u * nl);
                 }
                 if (s.n_pad) encode_slot_scalar(s, d, row, [&](uint32_t col, float v) { st.one(r, col, v); });
@@ -501,7 +508,7 @@ template <int NL, int TPR, typename Store, typename TT>
 __device__ __forceinline__ void encode_row_part(const ModelDesc& d, const GridLevel* level_tables, const TT* __restrict__ params,
                                                 const float* in_s, uint32_t in_ld, const float* __restrict__ ml_gpu, float ml_scalar,
                                                 uint32_t row0, uint32_t r, uint32_t part, Store& st, const uint32_t* smem_tab = nullptr,
-                                                uint32_t smem_levels = 0, const uint4* cells = nullptr, uint32_t cells_levels = 0) {
+                                                uint32_t smem_levels = 0, CellTable ct = {}) {
     const float* row = in_s + r * in_ld;
     const float ml = ml_gpu ? __ldg(ml_gpu + row0 + r) : ml_scalar;
     const bool last = part == (uint32_t)(TPR - 1);
@@ -519,8 +526,8 @@ __device__ __forceinline__ void encode_row_part(const ModelDesc& d, const GridLe
             for (uint32_t l0 = lb; l0 < le; l0 += NL) {
                 float f[2 * NL];
                 const uint32_t nl = min((uint32_t)NL, le - l0);
-                grid_group_forward<NL, TT>(g, lv, l0, nl, table, px, py, pz, ml, f, smem_tab, s.grid == 0 ? smem_levels : 0u, cells,
-                                           s.grid == 0 ? cells_levels : 0u);
+                grid_group_forward<NL, TT>(g, lv, l0, nl, table, px, py, pz, ml, f, smem_tab, s.grid == 0 ? smem_levels : 0u,
+                                           s.grid == 0 ? ct : CellTable{});
                 st.run(r, s.out_begin + 2u * l0, f, 2u * nl);
             }
             if (last && s.n_pad) encode_slot_scalar(s, d, row, [&](uint32_t col, float v) { st.one(r, col, v); });

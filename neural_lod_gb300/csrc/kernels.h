@@ -55,9 +55,10 @@ struct ForwardArgs {
     const float* params;              // FP32 parameters (network then encoding)
     const void* weights_op;           // network weights in the operand type (FP16/BF16 forms)
     const void* grid_h;               // FP16 copy of the parameters' grid tables (FP16 tensor-core inference)
-    const void* cells;                // nullable: cell table of grid_h's leading dense levels (build_cells)
+    const void* cells;                // nullable: cell table of grid_h's leading levels (cells.cu)
     uint32_t cells_levels;            // levels of the first grid that the cell table covers
     const uint32_t* cells_stale;      // device word: nonzero while the table lags grid_h (then unused)
+    uint32_t cell_base[kMaxLevels];   // first record of each covered level
     const float* max_level_gpu;       // nullable, [n]
     float max_level;                  // scalar fallback (1000 = off)
     float* out;                       // nullable, [n][n_output]
@@ -179,15 +180,16 @@ bool tc_variant_ok(const ModelDesc& d, int variant, int kind = 1);
 int tc_default_variant(const ModelDesc& d);
 cudaError_t launch_forward_tc(const ModelDesc& d, const ForwardArgs& a, int kind, int variant, uint32_t* status, cudaStream_t s);
 
-// cells.cu: the cell table of the first grid's leading dense levels (FP16 tables).
-// Levels it covers (0: none), its 32-byte records, and the (re)build from the FP16 copy grid_h.
-uint32_t cells_levels_of(const ModelDesc& d);
-size_t cells_records(const ModelDesc& d, uint32_t levels);
-cudaError_t launch_build_cells(const ModelDesc& d, const void* grid_h, uint32_t levels, void* cells, cudaStream_t s);
+// cells.cu: the cell table of the first grid's leading levels (FP16 tables), its (re)build from
+// the FP16 copy grid_h.
+// Levels it covers (0: none) and their record bases (base[l], base[levels] = all records).
+uint32_t cells_levels_of(const ModelDesc& d, uint32_t (&base)[kMaxLevels + 1]);
+cudaError_t launch_build_cells(const ModelDesc& d, const void* grid_h, uint32_t levels, const uint32_t (&base)[kMaxLevels + 1], void* cells,
+                               cudaStream_t s);
 
 // calib.cu
 cudaError_t launch_calib_gathers(const ModelDesc& d, const void* params, bool half_tables, uint32_t n, float* sink, cudaStream_t s,
-                                 const void* cells = nullptr, uint32_t cells_levels = 0);
+                                 const void* cells = nullptr, uint32_t cells_levels = 0, const uint32_t* cell_base = nullptr);
 cudaError_t launch_calib_scatter(const ModelDesc& d, float* grads, uint32_t n, cudaStream_t s);
 
 // Fused tensor-core training step (train_tc.cu): encoding, forward, loss, backward, weight

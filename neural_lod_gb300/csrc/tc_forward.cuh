@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(G * kGroupThreads * TPR, (G * TPR == 2 ? 2 : 1
     const uint32_t n_tiles = aborted ? 0u : forward_rows(a) / kTcTile;
     // the cell table of the FP16 tables, unless an optimizer step has changed them since it was
     // built (the corners are then gathered)
-    const uint4* cells = a.cells && __ldg(a.cells_stale) == 0u ? static_cast<const uint4*>(a.cells) : nullptr;
+    const CellTable cells{a.cells && __ldg(a.cells_stale) == 0u ? static_cast<const uint4*>(a.cells) : nullptr, a.cell_base, a.cells_levels};
     const uint32_t row = quarter * 32u + lane;   // TMEM lane == tile row owned in the epilogue
     const uint32_t taddr_row = tmem_base + ((quarter * 32u) << 16);
 
@@ -223,12 +223,12 @@ __global__ void __launch_bounds__(G * kGroupThreads * TPR, (G * TPR == 2 ? 2 : 1
             if constexpr (TPR > 1) {
                 if constexpr (std::is_same<T, __half>::value)
                     encode_row_part<NL, TPR>(d, lvl_s, static_cast<const __half*>(a.grid_h), in_s, L.in_ld, a.max_level_gpu, a.max_level, row0,
-                                             gtid & 127u, part, st, tab_s, L.tab_levels, cells, cells ? a.cells_levels : 0u);
+                                             gtid & 127u, part, st, tab_s, L.tab_levels, cells);
                 else
                     encode_row_part<NL, TPR>(d, lvl_s, a.params, in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, gtid & 127u, part, st);
             } else if constexpr (std::is_same<T, __half>::value) {
                 encode_tile_rows<NL>(d, lvl_s, static_cast<const __half*>(a.grid_h), in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile,
-                                     gtid, kGroupThreads, st, tab_s, L.tab_levels, cells, cells ? a.cells_levels : 0u);
+                                     gtid, kGroupThreads, st, tab_s, L.tab_levels, cells);
             } else {
                 encode_tile_rows<NL>(d, lvl_s, a.params, in_s, L.in_ld, a.max_level_gpu, a.max_level, row0, kTcTile, gtid, kGroupThreads, st);
             }
