@@ -240,8 +240,8 @@ def test_deterministic(cuda, nlod_lib):
 
 @pytest.mark.parametrize("precision", ["fp16", "fp32"])
 def test_inference_from_host_buffers(cuda, nlod_lib, precision):
-    """nlod_inference_host: a pinned input read in place, a pageable one staged; both give the
-    device call's outputs bit for bit."""
+    """nlod_inference_host: a pinned input read in place, a pageable one staged; pinned and
+    pageable outputs; every combination gives the device call's outputs bit for bit."""
     import torch
 
     m, _, _ = _net(W.throughput_configs(), 10, 3, precision, grid_scale=0.2)
@@ -254,6 +254,14 @@ def test_inference_from_host_buffers(cuda, nlod_lib, precision):
     m.inference_host(xh.clone(), out)
     torch.cuda.synchronize()
     assert torch.equal(out, ref)
+    out2 = torch.zeros((8192, 3), dtype=torch.float32)       # pinned input, pageable output
+    m.inference_host(xh.pin_memory(), out2)
+    torch.cuda.synchronize()
+    assert torch.equal(out2, ref)
+    out3 = torch.zeros((8192, 3), dtype=torch.float32).pin_memory()   # pageable input, pinned output
+    m.inference_host(xh.clone(), out3)
+    torch.cuda.synchronize()
+    assert torch.equal(out3, ref)
     with pytest.raises(ValueError):
         m.inference_host(xh.to(cuda))
 
