@@ -34,3 +34,23 @@ def test_background_and_caps():
     assert tot[0] > 0 and tot[1] > 0
     img2, st2, _ = oracle.render(vo, vp, to, tp, lvl, P, CAM)
     assert np.array_equal(img, img2) and np.array_equal(st, st2)
+
+
+def test_render_params_validation_on_the_host(nlod_lib):
+    """nlod_render_camera validates the parameters without a GPU: the query-chain cap accepts 0-64
+    (0: the default of 8), the struct keeps its size with the cap in the former padding."""
+    import ctypes as C
+
+    from neural_lod_gb300 import NlodError
+    from neural_lod_gb300.render import _Params, camera
+
+    assert C.sizeof(_Params) == 112
+    for mc in (0, 1, 8, 64):
+        cam = camera(RenderParams(width=16, height=8, level=0, max_chain=mc), 32)
+        assert np.all(np.isfinite(cam))
+    try:
+        camera(RenderParams(width=16, height=8, level=0, max_chain=65), 32)
+    except NlodError as e:
+        assert e.code == 1 and "max_chain" in str(e)
+    else:
+        raise AssertionError("max_chain 65 accepted")
