@@ -264,6 +264,13 @@ def test_inference_from_host_buffers(cuda, nlod_lib, precision):
     assert torch.equal(out3, ref)
     with pytest.raises(ValueError):
         m.inference_host(xh.to(cuda))
+    # a large batch
+    nb = (1 << 19) + 128 * 7
+    xb = torch.from_numpy(W.throughput_inputs(nb, seed=10))
+    refb = m.inference(xb.to(cuda)).cpu()
+    outb = m.inference_host(xb.pin_memory())
+    torch.cuda.synchronize()
+    assert torch.equal(outb, refb)
 
 
 @pytest.mark.parametrize("with_ema", [False, True])
