@@ -114,6 +114,20 @@ enum : uint32_t { CHAIN_OPEN = 0, CHAIN_DONE = 1, CHAIN_DROPPED = 2, CHAIN_FAIL 
 constexpr uint32_t kThrDeferBelow = 32768u;
 constexpr uint32_t kThrDeferRounds = 8u;
 
+// The pixel that ray generation's thread j takes: strips of four rows, each walked column by
+// column, so that a warp's 32 rays cover 8 x 4 pixels (their directions, and with them the
+// distances they march, are closer than along 32 pixels of one row).  The ray's index stays its
+// pixel's, which keys its image entry, counts and sampled directions, so the order changes
+// nothing but the lists' initial order.  Frame (1024^2): 6.33 ms with one row, 6.23 ms with
+// strips of 4 rows, 6.41 / 6.58 / 6.66 ms with 8 / 16 / 32.
+constexpr uint32_t kStripRows = 4u;
+__device__ __forceinline__ uint32_t tiled_pixel(const RenderConsts& C, uint32_t j) {
+    const uint32_t strip = j / (kStripRows * C.width);
+    const uint32_t rows = min(kStripRows, C.height - kStripRows * strip);
+    const uint32_t idx = j - strip * kStripRows * C.width;
+    return (kStripRows * strip + idx % rows) * C.width + idx / rows;
+}
+
 // The end of a march that produced no query: the escaped ray's pixel, a dropped ray or a failed
 // traversal.
 __device__ __forceinline__ void march_end(const RenderConsts& C, const RenderBufs& B, const RayState& st, uint32_t ray, uint32_t end) {
@@ -155,8 +169,8 @@ __global__ void __launch_bounds__(256, 4) k_step(const __grid_constant__ RenderC
         if (valid) {
             bool march = false;
             if (first) {
-                ray = j;
-                ray_generate(C, j, st);
+                ray = tiled_pixel(C, j);
+                ray_generate(C, ray, st);
 #pragma unroll
                 for (int k = 0; k < 3; ++k) B.image[3 * ray + k] = 0.f;
                 B.ray_stats[2 * ray] = 0u;
