@@ -203,8 +203,9 @@ def test_training_step_graph_matches_direct_launches(cuda, nlod_lib, with_ema):
     CUDA graph updated per call; on the legacy default stream it is launched directly.  Over steps
     that change the inputs, the batch size and whether a loss is returned, both give the same
     losses and parameters up to the order of the gradient reductions (FP32 atomics, whose order
-    differs from run to run): losses within 1e-4 relative, parameters within 1e-2 of the
-    trajectory's total update."""
+    differs from run to run): losses within 1e-4 relative, parameters within 2e-2 of the
+    trajectory's total update (the difference between two runs of either form is of the same size:
+    up to 1.1 % measured with the EMA over these ten steps)."""
     import torch
 
     enc, net = W.throughput_configs()
@@ -237,4 +238,4 @@ def test_training_step_graph_matches_direct_launches(cuda, nlod_lib, with_ema):
     for a, b in ((pg, pd), (ig, id_)):
         moved = np.linalg.norm(b.astype(np.float64) - params)
         assert moved > 0
-        assert np.linalg.norm(a.astype(np.float64) - b) <= 1e-2 * moved
+        assert np.linalg.norm(a.astype(np.float64) - b) <= 2e-2 * moved
