@@ -334,7 +334,10 @@ typedef struct nlod_render_params {
                                       autotuned) and the wavefront rounds, timed on this scene at
                                       creation; else the wavefront rounds.
                                       NLOD_RENDER_WAVEFRONT / NLOD_RENDER_PERSISTENT force one form;
-                                      NLOD_RENDER_HOST_ROUNDS issues the wavefront rounds from the host */
+                                      NLOD_RENDER_HOST_ROUNDS issues the wavefront rounds from the host.
+                                      The wavefront form (AUTO, WAVEFRONT) also picks its modules'
+                                      inference kernel organisations for this frame by timing frames
+                                      at creation; the modules' own settings are unchanged */
     uint32_t max_chain;            /* wavefront forms: most visibility queries a ray marches ahead in one
                                       round (query k+1 is the march that follows query k's rejection; the
                                       queries past an accepted one are dropped, so pixels and counts do not

@@ -303,15 +303,23 @@ namespace nlod {
 
 // Inference launch used by the wavefront renderer: inference parameters, a scalar max level, and
 // the row count read from device memory at launch time (n_max rows of input/output storage).
+// variant: the tensor-core kernel organisation (< 0: the module's own).
 cudaError_t module_inference_device_count(nlod_module* m, uint32_t n_max, const float* in, float* out, const uint32_t* n_dev,
-                                          float max_level, cudaStream_t s) {
+                                          float max_level, cudaStream_t s, int variant) {
     ForwardArgs a = base_forward_args(m, n_max, in, true);
     a.out = out;
     a.n_dev = n_dev;
     a.max_level_gpu = nullptr;
     a.max_level = max_level;
     if (m->precision == NLOD_PRECISION_FP32) return launch_forward_simt(m->d, a, 0, s);
-    return launch_forward_tc(m->d, a, m->op_kind(), m->tc_variant, m->status, s);
+    return launch_forward_tc(m->d, a, m->op_kind(), variant < 0 ? m->tc_variant : variant, m->status, s);
+}
+
+// The module's own tensor-core kernel organisation (-1 for the FP32 form), and whether another
+// one fits it.
+int module_variant(nlod_module* m) { return m->precision == NLOD_PRECISION_FP32 ? -1 : m->tc_variant; }
+bool module_variant_ok(nlod_module* m, int variant) {
+    return m->precision != NLOD_PRECISION_FP32 && variant >= 0 && tc_variant_ok(m->d, variant, m->op_kind());
 }
 
 uint32_t* module_status_word(nlod_module* m) { return m->status; }

@@ -46,7 +46,9 @@ struct nlod_module;
 namespace nlod {
 
 cudaError_t module_inference_device_count(nlod_module* m, uint32_t n_max, const float* in, float* out, const uint32_t* n_dev,
-                                          float max_level, cudaStream_t s);
+                                          float max_level, cudaStream_t s, int variant = -1);
+int module_variant(nlod_module* m);
+bool module_variant_ok(nlod_module* m, int variant);
 bool module_tc_operands(nlod_module* m, const ModelDesc** d, const void** weights, const void** table, int* kind);
 cudaError_t module_prepare_inference(nlod_module* m, cudaStream_t s);
 
@@ -394,6 +396,7 @@ struct nlod_renderer {
     float vis_max_level = 1000.f;
     int mode = NLOD_RENDER_WAVEFRONT;
     int pk_groups = 0;              // tile pipelines per CTA of the persistent form (autotuned)
+    int vis_variant = -1, thr_variant = -1;   // the wavefront forms' inference organisations (-1: the module's)
     unsigned step_blocks = 0;       // k_step grid of the wavefront forms
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
@@ -657,53 +660,107 @@ int nlod_renderer_create(nlod_module* visibility, nlod_module* throughput, const
             const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 152ull * 32);
             r->step_blocks = blocks;
             if (p->mode == NLOD_RENDER_HOST_ROUNDS) r->mode = NLOD_RENDER_HOST_ROUNDS;
-            cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
-            k_reset<<<1, 1, 0, s>>>(B.ctl);
-            k_step<<<blocks, 256, 0, s>>>(C, B, 1);
-            k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, C.max_chain, B.status, 0, 0, 0);
-            cudaStreamCaptureStatus cst;
-            cudaGraph_t cap_graph = nullptr;
-            const cudaGraphNode_t* deps = nullptr;
-            size_t n_deps = 0;
-            cuda_check(cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap_graph, &deps, nullptr, &n_deps), "capture info");
-            cudaGraphConditionalHandle cond;
-            cuda_check(cudaGraphConditionalHandleCreate(&cond, cap_graph, 1, cudaGraphCondAssignDefault), "conditional handle");
-            cudaGraphNodeParams cp{};
-            cp.type = cudaGraphNodeTypeConditional;
-            cp.conditional.handle = cond;
-            cp.conditional.type = cudaGraphCondTypeWhile;
-            cp.conditional.size = 1;
-            cudaGraphNode_t loop_node;
-            cuda_check(cudaGraphAddNode(&loop_node, cap_graph, deps, nullptr, n_deps, &cp), "conditional node");
-            cuda_check(cudaStreamUpdateCaptureDependencies(s, &loop_node, nullptr, 1, cudaStreamSetCaptureDependencies), "capture deps");
-            cudaGraph_t body = cp.conditional.phGraph_out[0];
-            cudaStream_t bs;
-            cuda_check(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking), "stream");
-            cudaError_t e = cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-            if (e == cudaSuccess) {
-                e = module_inference_device_count(r->vis, r->vis_rows_max, B.vis_in, B.vis_out, &B.ctl->n_rows, r->vis_max_level, bs);
-                // the throughput inference inside an if node: most rounds carry its list over (or
-                // have none), and a launch that finds no rows still costs its grid's start-up
-                cudaGraphConditionalHandle thr_cond{};
-                if (e == cudaSuccess) e = add_conditional_body(bs, cudaGraphCondTypeIf, &thr_cond, [&](cudaStream_t ts) {
-                    return module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, ts);
-                });
+            // Records the frame graph with the given inference organisations into r->graph / r->exec.
+            auto capture = [&](int vv, int tv) {
+                if (r->exec) cudaGraphExecDestroy(r->exec);
+                if (r->graph) cudaGraphDestroy(r->graph);
+                r->exec = nullptr;
+                r->graph = nullptr;
+                r->vis_variant = vv;
+                r->thr_variant = tv;
+                cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "capture");
+                k_reset<<<1, 1, 0, s>>>(B.ctl);
+                k_step<<<blocks, 256, 0, s>>>(C, B, 1);
+                k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, C.max_chain, B.status, 0, 0, 0);
+                cudaStreamCaptureStatus cst;
+                cudaGraph_t cap_graph = nullptr;
+                const cudaGraphNode_t* deps = nullptr;
+                size_t n_deps = 0;
+                cuda_check(cudaStreamGetCaptureInfo(s, &cst, nullptr, &cap_graph, &deps, nullptr, &n_deps), "capture info");
+                cudaGraphConditionalHandle cond;
+                cuda_check(cudaGraphConditionalHandleCreate(&cond, cap_graph, 1, cudaGraphCondAssignDefault), "conditional handle");
+                cudaGraphNodeParams cp{};
+                cp.type = cudaGraphNodeTypeConditional;
+                cp.conditional.handle = cond;
+                cp.conditional.type = cudaGraphCondTypeWhile;
+                cp.conditional.size = 1;
+                cudaGraphNode_t loop_node;
+                cuda_check(cudaGraphAddNode(&loop_node, cap_graph, deps, nullptr, n_deps, &cp), "conditional node");
+                cuda_check(cudaStreamUpdateCaptureDependencies(s, &loop_node, nullptr, 1, cudaStreamSetCaptureDependencies), "capture deps");
+                cudaGraph_t body = cp.conditional.phGraph_out[0];
+                cudaStream_t bs;
+                cuda_check(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking), "stream");
+                cudaError_t e = cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
                 if (e == cudaSuccess) {
-                    k_step<<<blocks, 256, 0, bs>>>(C, B, 0);
-                    k_round<<<1, 1, 0, bs>>>(B.ctl, C.max_rounds, C.max_chain, B.status, cond, thr_cond, 1);
-                    e = cudaGetLastError();
+                    e = module_inference_device_count(r->vis, r->vis_rows_max, B.vis_in, B.vis_out, &B.ctl->n_rows, r->vis_max_level, bs, vv);
+                    // the throughput inference inside an if node: most rounds carry its list over
+                    // (or have none), and a launch that finds no rows still costs its grid's start-up
+                    cudaGraphConditionalHandle thr_cond{};
+                    if (e == cudaSuccess) e = add_conditional_body(bs, cudaGraphCondTypeIf, &thr_cond, [&](cudaStream_t ts) {
+                        return module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, ts, tv);
+                    });
+                    if (e == cudaSuccess) {
+                        k_step<<<blocks, 256, 0, bs>>>(C, B, 0);
+                        k_round<<<1, 1, 0, bs>>>(B.ctl, C.max_rounds, C.max_chain, B.status, cond, thr_cond, 1);
+                        e = cudaGetLastError();
+                    }
+                    cudaGraph_t body_out = body;
+                    const cudaError_t e2 = cudaStreamEndCapture(bs, &body_out);
+                    if (e == cudaSuccess) e = e2;
                 }
-                cudaGraph_t body_out = body;
-                const cudaError_t e2 = cudaStreamEndCapture(bs, &body_out);
-                if (e == cudaSuccess) e = e2;
+                cudaStreamDestroy(bs);
+                cudaGraph_t g = nullptr;
+                const cudaError_t e3 = cudaStreamEndCapture(s, &g);
+                r->graph = g;
+                cuda_check(e, "frame graph body");
+                cuda_check(e3, "frame graph");
+                cuda_check(cudaGraphInstantiate(&r->exec, r->graph, 0), "graph instantiate");
+            };
+            capture(-1, -1);
+            if (p->mode != NLOD_RENDER_HOST_ROUNDS && module_variant(r->vis) >= 0 && module_variant(r->thr) >= 0) {
+                // The inference organisations for this frame: the modules' own (tuned on batches of
+                // their own) against the ones that suit the frame's rounds (four and six pipelines
+                // with two and one threads per tile row), one network at a time, each timed on a
+                // frame of its graph after a warm-up frame.  The modules' settings are unchanged.
+                cudaEvent_t e0, e1;
+                cuda_check(cudaEventCreate(&e0), "event");
+                cuda_check(cudaEventCreate(&e1), "event");
+                auto frame_ms = [&]() {
+                    float ms = 3.0e38f;
+                    if (cudaGraphLaunch(r->exec, s) == cudaSuccess && cudaEventRecord(e0, s) == cudaSuccess &&
+                        cudaGraphLaunch(r->exec, s) == cudaSuccess && cudaEventRecord(e1, s) == cudaSuccess &&
+                        cudaEventSynchronize(e1) == cudaSuccess)
+                        cudaEventElapsedTime(&ms, e0, e1);
+                    return ms;
+                };
+                const int own_v = module_variant(r->vis), own_t = module_variant(r->thr);
+                const uint32_t* no_rows = static_cast<const uint32_t*>(alloc(sizeof(uint32_t)));   // a zero row count
+                int best_v = own_v, best_t = own_t;
+                float best = frame_ms();
+                for (int which = 0; which < 2; ++which) {
+                    nlod_module* m = which == 0 ? r->thr : r->vis;
+                    const int own = which == 0 ? own_t : own_v;
+                    for (int cand : {12, 6}) {
+                        if (cand == own || !module_variant_ok(m, cand)) continue;
+                        const int vv = which == 0 ? best_v : cand, tv = which == 0 ? cand : best_t;
+                        // zero-row launch outside the capture: the kernel's shared-memory attribute
+                        cuda_check(module_inference_device_count(m, which == 0 ? r->n_pad : r->vis_rows_max, which == 0 ? B.thr_in : B.vis_in,
+                                                                 which == 0 ? B.thr_out : B.vis_out, no_rows, 1000.f, s, cand),
+                                   "inference");
+                        capture(vv, tv);
+                        const float ms = frame_ms();
+                        if (ms < best) {
+                            best = ms;
+                            best_v = vv;
+                            best_t = tv;
+                        }
+                    }
+                }
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                cuda_check(cudaStreamSynchronize(s), "synchronize");
+                if (best_v != r->vis_variant || best_t != r->thr_variant) capture(best_v == own_v ? -1 : best_v, best_t == own_t ? -1 : best_t);
             }
-            cudaStreamDestroy(bs);
-            cudaGraph_t g = nullptr;
-            const cudaError_t e3 = cudaStreamEndCapture(s, &g);
-            r->graph = g;
-            cuda_check(e, "frame graph body");
-            cuda_check(e3, "frame graph");
-            cuda_check(cudaGraphInstantiate(&r->exec, r->graph, 0), "graph instantiate");
         } catch (...) {
             nlod_renderer_destroy(r.release());
             throw;
@@ -732,8 +789,10 @@ int nlod_render_frame(nlod_renderer* r, void* stream, float* image, uint32_t* ra
                 cuda_check(cudaMemcpyAsync(&c, B.ctl, sizeof c, cudaMemcpyDeviceToHost, s), "copy");
                 cuda_check(cudaStreamSynchronize(s), "synchronize");
                 if (c.n_vis + c.n_thr == 0 || c.round > C.max_rounds) break;
-                cuda_check(module_inference_device_count(r->vis, r->vis_rows_max, B.vis_in, B.vis_out, &B.ctl->n_rows, r->vis_max_level, s), "inference");
-                cuda_check(module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, s), "inference");
+                cuda_check(module_inference_device_count(r->vis, r->vis_rows_max, B.vis_in, B.vis_out, &B.ctl->n_rows, r->vis_max_level, s,
+                                                         r->vis_variant), "inference");
+                cuda_check(module_inference_device_count(r->thr, r->n_pad, B.thr_in, B.thr_out, &B.ctl->thr_rows, 1000.f, s, r->thr_variant),
+                           "inference");
                 k_step<<<r->step_blocks, 256, 0, s>>>(C, B, 0);
                 k_round<<<1, 1, 0, s>>>(B.ctl, C.max_rounds, C.max_chain, B.status, 0, 0, 0);
                 cuda_check(cudaGetLastError(), "launch");
