@@ -71,6 +71,7 @@ struct nlod_module {
     void* w_op = nullptr;           // operand copy (FP16/BF16) of the network part of `params`
     void* w_op_inf = nullptr;       // operand copy of the inference network weights
     uint16_t* grid_h = nullptr;     // FP16 copy of the inference parameters (grid part used), FP16 modules with grids
+    uint16_t* grid_b_train = nullptr;   // BF16 copy of the training values (grid part), BF16 modules with grids
     // Cell table of grid_h's leading levels (cells.cu).  An optimizer step marks it out of
     // date on the device (cells_stale, which the kernels read before using it) and on the host
     // (cells_dirty); the next inference call rebuilds it, so training steps do not pay for it and
@@ -154,6 +155,10 @@ void ensure_cells(nlod_module* m, cudaStream_t s) {
 // them in its own pass).
 void refresh_operand_copies(nlod_module* m, cudaStream_t s) {
     if (m->precision == NLOD_PRECISION_FP32) return;
+    if (m->grid_b_train) {
+        const uint32_t off = m->d.n_params_network, n = (uint32_t)(m->d.n_params - m->d.n_params_network);
+        cuda_check(launch_convert_weights(m->params + off, m->grid_b_train + off, n, 2, s), "convert grid tables");
+    }
     cuda_check(launch_convert_weights(m->params, m->w_op, m->d.n_params_network, m->op_kind(), s), "convert weights");
     if (m->w_op_inf != m->w_op)
         cuda_check(launch_convert_weights(m->ema, m->w_op_inf, m->d.n_params_network, m->op_kind(), s), "convert inference weights");
@@ -276,6 +281,7 @@ void run_optimizer(nlod_module* m, cudaStream_t s) {
     // the same pass refreshes every derived copy: operand-type weights and the FP16 grid tables
     a.grid_h = reinterpret_cast<__half*>(m->grid_h);
     a.grid_h_train = reinterpret_cast<__half*>(m->grid_h_train);
+    a.grid_b_train = reinterpret_cast<__nv_bfloat16*>(m->grid_b_train);
     a.w_op = m->precision == NLOD_PRECISION_FP32 ? nullptr : m->w_op;
     a.w_op_inf = m->precision == NLOD_PRECISION_FP32 ? nullptr : m->w_op_inf;
     a.op_kind = m->op_kind();
@@ -434,6 +440,7 @@ int nlod_module_create(const char* encoding_json, const char* network_json, cons
                 m->w_op = dev_alloc<uint16_t>(m->d.n_params_network);
                 m->w_op_inf = m->ema ? dev_alloc<uint16_t>(m->d.n_params_network) : m->w_op;
             }
+            if (precision == NLOD_PRECISION_BF16 && m->d.n_grids > 0 && m->has_loss) m->grid_b_train = dev_alloc<uint16_t>(np);
             if (precision == NLOD_PRECISION_FP16 && m->d.n_grids > 0) {
                 m->grid_h = dev_alloc<uint16_t>(np);
                 if (m->ema) m->grid_h_train = dev_alloc<uint16_t>(np);
@@ -542,6 +549,7 @@ void nlod_module_destroy(nlod_module* m) {
     if (m->w_op_inf != m->w_op) dev_free(m->w_op_inf);
     dev_free(m->grid_h);
     dev_free(m->grid_h_train);
+    dev_free(m->grid_b_train);
     dev_free(m->cells);
     dev_free(m->cells_stale);
     dev_free(m->w_op);
@@ -754,7 +762,8 @@ static int train_impl(nlod_module* m, void* stream, uint32_t n, const float* in,
             t.grads = m->grads;
             t.loss_partial = m->loss_partial;
             // FP16 training values: the inference copy without an EMA, the separate training copy with one
-            t.grid_h = m->ema ? m->grid_h_train : m->grid_h;
+            t.grid_h = m->grid_b_train ? static_cast<const void*>(m->grid_b_train)
+                                       : m->ema ? static_cast<const void*>(m->grid_h_train) : static_cast<const void*>(m->grid_h);
             // the encoding kernel zeroes the gradients (4-float tail, if any, by a memset)
             t.zero_grads_n = (uint32_t)(m->n_params & ~size_t(3));
             const size_t enc_bytes = (size_t)n * m->d.enc_width * 2u;

@@ -16,6 +16,7 @@
 // consuming kernel) receives the features.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <cstdint>
@@ -148,6 +149,23 @@ __device__ __forceinline__ void table_pair(const __half* t, uint32_t even, float
     lo = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
     hi = __half22float2(*reinterpret_cast<const __half2*>(&q.y));
 }
+__device__ __forceinline__ float2 table_entry(const __nv_bfloat16* t, uint32_t e) {
+    const uint32_t w = __ldg(reinterpret_cast<const unsigned int*>(t) + e);
+    return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w));
+}
+__device__ __forceinline__ void table_pair(const __nv_bfloat16* t, uint32_t even, float2& lo, float2& hi) {
+    const uint2 q = __ldg(reinterpret_cast<const uint2*>(t) + (even >> 1));
+    lo = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.x));
+    hi = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.y));
+}
+// Entries a and b of one aligned block of four BF16 entries {4m .. 4m+3} with one 16-byte load.
+__device__ __forceinline__ void table_quad(const __nv_bfloat16* t, uint32_t a, uint32_t b, float2& va, float2& vb) {
+    const uint4 q = __ldg(reinterpret_cast<const uint4*>(t) + (a >> 2));
+    const uint32_t wa = (a & 2u) ? ((a & 1u) ? q.w : q.z) : ((a & 1u) ? q.y : q.x);
+    const uint32_t wb = (b & 2u) ? ((b & 1u) ? q.w : q.z) : ((b & 1u) ? q.y : q.x);
+    va = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&wa));
+    vb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&wb));
+}
 // Entries a and b of one aligned block of four FP16 entries {4m .. 4m+3} with one 16-byte load.
 __device__ __forceinline__ void table_quad(const __half* t, uint32_t a, uint32_t b, float2& va, float2& vb) {
     const uint4 q = __ldg(reinterpret_cast<const uint4*>(t) + (a >> 2));
@@ -217,15 +235,15 @@ __device__ __forceinline__ void grid_group_forward(const GridDesc& g, const Grid
                 uint32_t e[8];
                 level_corner_entries(L, p0, p1, p2, cx, cy, cz, e);
                 // x-adjacent corners whose entries lie in one aligned block come in one load:
-                // a pair {2m, 2m+1} of FP32 entries in 16 bytes, a block {4m .. 4m+3} of FP16
-                // entries in 16 bytes (3 in 4 x-pairs of the coherent-prime hash and of dense
+                // a pair {2m, 2m+1} of FP32 entries in 16 bytes, a block {4m .. 4m+3} of 16-bit
+                // (FP16 or BF16) entries in 16 bytes (3 in 4 x-pairs of the coherent-prime hash and of dense
                 // levels, against 1 in 2 for 8-byte pairs; measured -8 % in the gathers).  Every
                 // level starts on a multiple of 8 entries.
 #pragma unroll
                 for (int c = 0; c < 8; c += 2) {
                     const uint32_t ea = e[c], eb = e[c + 1];
-                    if constexpr (std::is_same<TT, __half>::value) {
-                        if (l < smem_levels) {
+                    if constexpr (sizeof(TT) == 2) {
+                        if (std::is_same<TT, __half>::value && l < smem_levels) {
                             // a level staged in shared memory: one FP16 pair per 32-bit word
                             const uint32_t* sl = smem_tab + L.offset;
                             const uint32_t wa = sl[ea], wb = sl[eb];

@@ -2,6 +2,7 @@
 // validate nothing (the C ABI validates first) and return the cudaError_t of the launch.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -156,6 +157,9 @@ struct AdamStepArgs {
     // nullable: FP16 copy of the training values of the non-matrix parameters, kept apart from
     // grid_h when an EMA makes the inference values differ (the FP16 training step gathers from it)
     __half* grid_h_train;
+    // nullable: BF16 copy of the training values of the non-matrix parameters (the BF16 training
+    // step gathers from it)
+    __nv_bfloat16* grid_b_train;
     // nullable: operand-type copies of the matrix parameters (training values, inference values),
     // refreshed in the same pass; op_kind 1 = FP16, 2 = BF16
     void* w_op;
@@ -210,8 +214,8 @@ struct TrainTcArgs {
     float* loss_partial;              // [gridDim.x] per-CTA loss sums (nullable)
     void* enc_tiles;                  // [n/128][128 x enc_width] operand-type X0 tiles written by
                                       // launch_encode_tiles and bulk-copied by the fused kernel
-    const void* grid_h;               // nullable: FP16 copy of the (training = inference) grid tables,
-                                      // read by launch_encode_tiles in the FP16 form
+    const void* grid_h;               // nullable: 16-bit copy of the training values' grid tables in
+                                      // the operand type (FP16 or BF16), read by launch_encode_tiles
     uint32_t zero_grads_n;            // launch_encode_tiles zeroes grads[0, zero_grads_n) (multiple of 4)
     uint32_t group_levels;            // grid levels a tile pipeline scatters itself when a
                                       // scatter team takes the rest (set by launch_train_tc)

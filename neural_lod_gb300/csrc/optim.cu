@@ -115,6 +115,13 @@ __global__ void __launch_bounds__(256) k_adam_step(const __grid_constant__ AdamS
             pk.y = *reinterpret_cast<const uint32_t*>(&hi);
             reinterpret_cast<uint2*>(a.grid_h_train)[q] = pk;
         }
+        if (a.grid_b_train && i0 >= a.n_matrix && (c0 | c1 | c2 | c3)) {
+            const __nv_bfloat162 lo = __floats2bfloat162_rn(w.x, w.y), hi = __floats2bfloat162_rn(w.z, w.w);
+            uint2 pk;
+            pk.x = *reinterpret_cast<const uint32_t*>(&lo);
+            pk.y = *reinterpret_cast<const uint32_t*>(&hi);
+            reinterpret_cast<uint2*>(a.grid_b_train)[q] = pk;
+        }
         return;
     }
     for (uint32_t i = i0; i < a.n_params; ++i) {
@@ -135,6 +142,7 @@ __global__ void __launch_bounds__(256) k_adam_step(const __grid_constant__ AdamS
         }
         if (a.grid_h && i >= a.n_matrix) a.grid_h[i] = __float2half_rn(inf);
         if (a.grid_h_train && i >= a.n_matrix && c) a.grid_h_train[i] = __float2half_rn(w);
+        if (a.grid_b_train && i >= a.n_matrix && c) a.grid_b_train[i] = __float2bfloat16_rn(w);
         if (i < a.n_matrix) {
             if (a.w_op && c) store_op1(a.w_op, i, w, a.op_kind);
             if (a.w_op_inf && a.w_op_inf != a.w_op) store_op1(a.w_op_inf, i, inf, a.op_kind);

@@ -695,8 +695,8 @@ __global__ void __launch_bounds__(G * kGT + 32 + (ST ? kGT : 0), 1)
 // Encoding of the batch into X0 tiles in HBM, each tile laid out exactly as the fused kernel's
 // shared-memory A operand (128 rows x enc_width, K-major core matrices), so that one bulk copy
 // brings it in.  Full occupancy (128-thread CTAs) for the gather-bound grid levels.
-// TT: element type of the grid tables gathered (float: the FP32 parameters; __half: their FP16
-// copy, a.grid_h).  One table type per instantiation keeps the gather code at its register count.
+// TT: element type of the grid tables gathered (float: the FP32 parameters; __half / __nv_bfloat16:
+// their 16-bit copy of the training values, a.grid_h).  One table type per instantiation keeps the gather code at its register count.
 template <typename T, int NL, typename TT>
 __global__ void __launch_bounds__(kTile) k_encode_tiles(const __grid_constant__ ModelDesc d, const __grid_constant__ TrainTcArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -727,7 +727,7 @@ __global__ void __launch_bounds__(kTile) k_encode_tiles(const __grid_constant__ 
         }
         __syncthreads();
         TcStore<T> st{reinterpret_cast<uint8_t*>(a.enc_tiles) + tile * x0_bytes, d.enc_width * 16u};
-        const TT* table = std::is_same<TT, __half>::value ? static_cast<const TT*>(a.grid_h) : reinterpret_cast<const TT*>(a.params);
+        const TT* table = std::is_same<TT, float>::value ? reinterpret_cast<const TT*>(a.params) : static_cast<const TT*>(a.grid_h);
         encode_tile_rows<NL>(d, lvl_s, table, in_s, in_ld, a.max_level_gpu, a.max_level, row0, kTile, tid, kTile, st);
     }
 }
@@ -847,6 +847,7 @@ cudaError_t launch_encode_tiles(const ModelDesc& d, const TrainTcArgs& a, int ki
     // equal to the inference values: no EMA)
     if (kind == 1 && a.grid_h) k_encode_tiles<__half, 2, __half><<<blocks, kTile, smem, s>>>(d, a);
     else if (kind == 1) k_encode_tiles<__half, 2, float><<<blocks, kTile, smem, s>>>(d, a);
+    else if (kind == 2 && a.grid_h) k_encode_tiles<__nv_bfloat16, 2, __nv_bfloat16><<<blocks, kTile, smem, s>>>(d, a);
     else if (kind == 2) k_encode_tiles<__nv_bfloat16, 2, float><<<blocks, kTile, smem, s>>>(d, a);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();

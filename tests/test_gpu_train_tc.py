@@ -11,9 +11,9 @@ Two references:
     16-bit operands themselves (at the random-target starting point of these tests the gradient
     sums cancel heavily), not of the kernel;
   * a float64 model of the same computation with the kernel's roundings (weights, encoded
-    features, activations, output gradients and deltas rounded to FP16 / BF16, and in the FP16
-    form the grid tables too, which it gathers from an FP16 copy of the training values (its own
-    copy when an EMA holds the inference values); everything
+    features, activations, output gradients and deltas rounded to FP16 / BF16, and the grid
+    tables too, which the encoding gathers from a 16-bit copy of the training values in the
+    operand type (the FP16 form's own copy when an EMA holds the inference values); everything
     else exact, products summed in float32): the network-weight gradients agree to about 1e-5
     relative, which pins the fused kernel's data flow.  The check allows 1e-2 (FP16) / 2e-2
     (BF16): a hidden pre-activation within rounding distance of zero can round to a different
@@ -42,14 +42,16 @@ def _round(a, precision):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-def _rounding_model(orc, spec, params, x, t, loss_name, precision, ml=None, fp16_tables=False):
-    """Network-weight gradients of the mean loss computed in float64 with the kernel's roundings."""
+def _rounding_model(orc, spec, params, x, t, loss_name, precision, ml=None, tables16=False):
+    """Network-weight gradients of the mean loss computed in float64 with the kernel's roundings.
+    The encoding gathers the grid tables from their 16-bit copy in the operand type (FP16 or
+    BF16), so the table values are rounded to it first."""
     q = lambda a: _round(a, precision)
     enc_params = params
-    if fp16_tables:
+    if tables16:
         n_net = spec["n_params_network"]
         enc_params = params.copy()
-        enc_params[n_net:] = params[n_net:].astype(np.float16).astype(np.float32)
+        enc_params[n_net:] = _round(params[n_net:], precision).astype(np.float32)
     x0 = q(orc.encode(x, enc_params, max_level=ml).astype(np.float64))
     ws = [q(params[L["offset"]:L["offset"] + L["in"] * L["out"]].reshape(L["out"], L["in"]).astype(np.float64)) for L in spec["layers"]]
     relu = spec["act"] == 1
@@ -108,7 +110,7 @@ def _check(m, orc, spec, params, x, t, loss_name, precision, cuda, ml=None, ema=
     untouched = ref_g[n_net:] == 0
     assert np.all(g[n_net:][untouched] == 0)
     # the same computation with the kernel's roundings, in float64
-    model = _rounding_model(orc, spec, params, x, t, loss_name, precision, ml, fp16_tables=precision == "fp16")
+    model = _rounding_model(orc, spec, params, x, t, loss_name, precision, ml, tables16=True)
     for L, gm in zip(spec["layers"], model):
         gl = g[L["offset"]:L["offset"] + L["in"] * L["out"]].reshape(L["out"], L["in"])
         e = _rel(gl, gm)
